@@ -1,0 +1,334 @@
+"""Benchmark of the Fenton-Karma stepper on the 2048x2048 roofline workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one bench "step"): a 2048x2048 float32 tissue with parameter set 3, diffusivity
+D = 0.001 (1 + 0.05 N(0,1)) clipped at 0 (seeded), a periodic left-edge stimulus (5 columns,
+amplitude 20, Protocol(start=0, duration=200, period=20000) in steps), advanced from rest through
+10 000 Euler steps (dt = dx = 0.01).  Inputs are synthetic and seeded.
+
+* ``value``        GCUPS (1e9 cell-updates/s) with the tissue resident in HBM, timed with CUDA
+                   events on the launching stream; L2 is flushed (256 MB write) between steps.
+* ``e2e``          the same metric through the public API (``solve.forward``) from pinned host
+                   arrays, host<->device copies of inputs and the returned state included.
+* ``roofline``     the step kernel against the measured HBM copy bandwidth: 28 algorithmic bytes
+                   per cell-update (read u, v, w, D; write u, v, w).
+* ``cpu_baseline`` the C restatement of the reference's stepper (the oracle port) on the host's
+                   cores, on a bounded sample of the same workload.
+
+``--impl reference`` times that CPU implementation alone on the same workload (the reference's
+own JAX CPU path cannot be installed here; the port is its restatement).  Multi-GPU runs are
+replicas (one tissue per rank, no data exchange): ``value`` sums all ranks' cell-updates over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_UPDATE = 28  # read u, v, w, D + write u, v, w (float32)
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload(H: int, W: int, seed: int = 1234):
+    rng = np.random.default_rng(seed)
+    D = np.clip(0.001 * (1.0 + 0.05 * rng.standard_normal((H, W))), 0.0, None).astype(np.float32)
+    field = np.zeros((H, W), np.float32)
+    field[:, :5] = 20.0
+    proto = (0, 200, 20000)
+    return D, field, proto
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(name: str):
+    """dram bytes per launch from a committed ncu summary (``dram_bytes_per_launch: N``)."""
+    path = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(path):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.proc, self.path = index, None, None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[0]) for r in rows if num(r[0]) is not None]
+        mx = [num(r[1]) for r in rows if num(r[1]) is not None]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in rows for n, v in zip(names, r[4:8]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_port_rate(H, W, D, field, proto, seconds: float, threads: int):
+    """GCUPS of the C oracle on a bounded sample (steps chosen to take about ``seconds``)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fk_oracle as O
+    import fk_oracle_c as C
+    C.build()
+    P3 = (3.33, 19.6, 1250, 870, 41, 0.25, 12.5, 33.33, 29, 10, 0.85, 0.13, 0.04, 1)
+    st = O.init((H, W))
+    stims = [(proto[0], proto[1], proto[2], field)]
+    t0 = time.perf_counter()
+    C.forward_euler(st, 0, 2, P3, D, stims, 0.01, 0.01, threads=threads)
+    per = max((time.perf_counter() - t0) / 2, 1e-4)
+    n = int(max(2, min(2000, seconds / per)))
+    t0 = time.perf_counter()
+    C.forward_euler(st, 0, n, P3, D, stims, 0.01, 0.01, threads=threads)
+    dt = time.perf_counter() - t0
+    return H * W * n / dt / 1e9, n, dt
+
+
+def run_reference(args):
+    """The CPU implementation (oracle port of cardiax/solve.py) on the same workload."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    H = W = args.size
+    D, field, proto = workload(H, W)
+    threads = os.cpu_count() or 1
+    rates, samples = [], []
+    for k in range(args.warmup + args.steps):
+        r, n, dt = cpu_port_rate(H, W, D, field, proto, args.cpu_seconds, threads)
+        if k >= args.warmup:
+            rates.append(r)
+            samples.append((n, dt))
+    total_updates = sum(H * W * n for n, _ in samples)
+    total_time = sum(dt for _, dt in samples)
+    value = total_updates / total_time / 1e9
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GCUPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * total_time / len(samples), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": config(args),
+        "cpu_baseline": {"value": value, "unit": "GCUPS", "cores": threads, "kind": "port",
+                         "sample": f"{H}x{W}, {samples[0][0]} Euler steps per sample, "
+                                   f"C restatement of cardiax/solve.py with OpenMP over rows"},
+        "e2e": {"value": value, "unit": "GCUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+METRIC = "GCUPS (1e9 Fenton-Karma cell-updates/s), fused FP32 Euler stepper; roofline.frac = % of HBM roofline"
+
+
+def config(args):
+    return {"workload": f"roofline_{args.size}: {args.size}x{args.size} FP32, PARAMSET_3, "
+                        f"D=0.001(1+0.05N(0,1)) clipped>=0, periodic left-edge stimulus "
+                        f"(5 columns, amplitude 20, Protocol(0,200,20000)), "
+                        f"{args.euler_steps} Euler steps from rest per bench step, dt=dx=0.01",
+            "H": args.size, "W": args.size, "euler_steps_per_step": args.euler_steps,
+            "l2": "flushed between timed steps (256 MB write)",
+            "kernel": "fk_step_kernel (one launch per Euler step)"}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    world, rank, local = dist_env()
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    from cardiax_gb300 import params, solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    from cardiax_gb300.tissue import Tissue
+
+    H = W = args.size
+    S = args.euler_steps
+    D, field, proto = workload(H, W, seed=1234 + rank)
+    P = params.PARAMSET_3
+    tis = Tissue((H, W), P, D, [Stimulus(Protocol(*proto), field)], dt=0.01, dx=0.01, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def one_step():
+        tis.init()
+        tis.advance(0, S)
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = Clocks(torch.cuda.current_device()).start()
+    t_wall = time.perf_counter()
+    evs = []
+    for k in range(args.steps):
+        flush.fill_(float(k))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        one_step()
+        e1.record()
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    updates = world * args.steps * H * W * S
+    value = updates / (ms / 1e3) / 1e9
+
+    # end to end through the public API from pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.as_tensor(a).pin_memory()  # noqa: E731
+        st0 = solve.State(pin(np.ones((H, W), np.float32)), pin(np.ones((H, W), np.float32)),
+                          pin(np.zeros((H, W), np.float32)))
+        Dp, fp = pin(D), pin(field)
+        h2d = 4 * H * W * 5  # v, w, u, D, stimulus field
+        d2h = 4 * H * W * 3  # returned v, w, u
+        times = []
+        for k in range(max(1, args.e2e_steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            states = solve.forward(st0, [0, S], P, Dp, [Stimulus(Protocol(*proto), fp)], 0.01,
+                                   0.01)
+            host = [x.cpu() for x in states[-1]]
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+            del states, host
+        e2e_s = sum(times)
+        if world > 1:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": world * len(times) * H * W * S / e2e_s / 1e9, "unit": "GCUPS",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    peak, peak_kind = peaks()
+    launch_ms = ms / (args.steps * S)
+    achieved = BYTES_PER_UPDATE * H * W / (launch_ms / 1e3) / 1e9
+    traffic = profiled_traffic(f"fk_step_kernel_{args.size}.md")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
+                if peak_kind == "measured" else "fallback 6800 GB/s",
+                "algorithmic_bytes_per_launch": BYTES_PER_UPDATE * H * W,
+                "avg_launch_us": launch_ms * 1e3}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        r, n, dt = cpu_port_rate(H, W, D, field, proto, args.cpu_seconds, threads)
+        cpu = {"value": r, "unit": "GCUPS", "cores": threads, "kind": "port",
+               "sample": f"{H}x{W}, {n} Euler steps ({dt:.1f} s), C restatement of "
+                         f"cardiax/solve.py with OpenMP over rows"}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+               "config": config(args), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+               "gpu_launches": args.steps * (S + 1), "clocks": clk,
+               "wall_s_timed_region": t_wall}
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--euler-steps", type=int, default=10000)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,11 @@
+"""cardiax_gb300: a GB300-native Fenton-Karma reaction-diffusion stepper.
+
+A drop-in for the forward path of epignatelli/cardiax (``cardiax.solve``): hand-written sm_103a
+CUDA kernels behind a C ABI (``include/cardiax_gb300.h``), driven from Python through ctypes on
+torch CUDA tensors and streams.
+"""
+from . import convert, params, stimulus  # noqa: F401
+from . import solve  # noqa: F401
+from .tissue import Tissue  # noqa: F401
+
+__all__ = ["convert", "params", "stimulus", "solve", "Tissue"]

@@ -1,0 +1,336 @@
+// C ABI of the single-tissue stepper: argument checks, TMA descriptors, step loops.
+//
+// Entry points and the reference functions they replace:
+//   fk_init           cardiax/solve.py:18-23   init
+//   fk_step           cardiax/solve.py:26-65   step (time derivative)
+//   fk_euler_step     cardiax/solve.py:68-70   step_euler
+//   fk_forward_euler  cardiax/solve.py:92-100  _forward_euler
+//   fk_forward        cardiax/solve.py:168-222 forward (Euler integrator)
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/cardiax_gb300.h"
+#include "fk_capi_internal.h"
+#include "fk_step.cuh"
+
+namespace fk {
+
+// ---- device error word ---------------------------------------------------------------------
+static __device__ int g_status_word;
+
+static std::mutex g_mu;
+static int *g_status_ptr[64];
+
+int *status_ptr() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_status_ptr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_status_word) != cudaSuccess) return nullptr;
+        g_status_ptr[dev] = static_cast<int *>(p);
+    }
+    return g_status_ptr[dev];
+}
+
+// ---- TMA descriptors ---------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+static bool encode_fn() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (g_encode) return true;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+        return false;
+    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    return true;
+}
+
+int make_plane_map(CUtensorMap *map, const float *plane, int64_t H, int64_t W, int64_t pitch,
+                   int box_w, int box_h) {
+    if (!encode_fn()) return FK_ERR_TENSORMAP;
+    cuuint64_t dims[2] = {(cuuint64_t)W, (cuuint64_t)H};
+    cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(plane),
+                          dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? FK_OK : FK_ERR_TENSORMAP;
+}
+
+// ---- argument preparation ----------------------------------------------------------------
+static inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+int check_grid(const fk_grid &g) {
+    if (g.H < 3 || g.W < 3 || g.pitch < g.W) return FK_ERR_SHAPE;
+    if (g.H > (1 << 24) || g.pitch > (1 << 24) || g.H * g.pitch > (int64_t(1) << 34))
+        return FK_ERR_SHAPE;
+    if (g.pitch % 4 != 0) return FK_ERR_ALIGN;
+    return FK_OK;
+}
+
+Model make_model(const fk_params &p) {
+    Model m{};
+    m.V_c = p.V_c;
+    m.V_v = p.V_v;
+    m.V_csi = p.V_csi;
+    m.k = p.k;
+    m.r_tau_d = 1.0f / p.tau_d;
+    m.r_tau_0 = 1.0f / p.tau_0;
+    m.inv_tau_r = 1.0f / p.tau_r;
+    m.r_2tau_si = 1.0f / (2.0f * p.tau_si);
+    m.r_Cm = 1.0f / p.Cm;
+    m.r_tau_v1m = 1.0f / p.tau_v1_minus;
+    m.r_tau_v2m = 1.0f / p.tau_v2_minus;
+    m.r_tau_vp = 1.0f / p.tau_v_plus;
+    m.r_tau_wm = 1.0f / p.tau_w_minus;
+    m.r_tau_wp = 1.0f / p.tau_w_plus;
+    return m;
+}
+
+int make_stims(const fk_stimulus *s, int n, const fk_grid &g, Stim *out) {
+    if (n < 0 || n > FK_MAX_STIMULI || n > kMaxStim) return FK_ERR_STIMULI;
+    if (n > 0 && !s) return FK_ERR_NULL;
+    for (int k = 0; k < n; ++k) {
+        if (!std::isfinite(s[k].start) || !std::isfinite(s[k].duration) ||
+            !std::isfinite(s[k].period) || s[k].period == 0.0)
+            return FK_ERR_STIMULI;
+        Stim &o = out[k];
+        o.start = (float)s[k].start;
+        o.duration = (float)s[k].duration;
+        o.period = (float)s[k].period;
+        o.amplitude = s[k].amplitude;
+        o.field = s[k].field;
+        o.field_plane = 0;
+        if (s[k].field) {
+            if (!aligned16(s[k].field)) return FK_ERR_ALIGN;
+            o.r0 = o.r1 = o.c0 = o.c1 = 0;
+        } else {
+            o.r0 = s[k].r0 < 0 ? 0 : s[k].r0;
+            o.r1 = s[k].r1 > g.H ? (int32_t)g.H : s[k].r1;
+            o.c0 = s[k].c0 < 0 ? 0 : s[k].c0;
+            o.c1 = s[k].c1 > g.W ? (int32_t)g.W : s[k].c1;
+        }
+    }
+    return FK_OK;
+}
+
+// Tensor maps of the u planes seen by one call (the ping-pong buffers and checkpoint slots).
+struct MapCache {
+    const float *ptr[4] = {nullptr, nullptr, nullptr, nullptr};
+    CUtensorMap map[4];
+    int next = 0;
+    int get(const fk_grid &g, const float *u, const CUtensorMap **out) {
+        for (int i = 0; i < 4; ++i)
+            if (ptr[i] == u) {
+                *out = &map[i];
+                return FK_OK;
+            }
+        const int k = next;
+        next = (next + 1) & 3;
+        int rc = make_plane_map(&map[k], u, g.H, g.W, g.pitch, SU_W, SU_H);
+        if (rc) return rc;
+        ptr[k] = u;
+        *out = &map[k];
+        return FK_OK;
+    }
+};
+
+// One step from `in` to `out` (Euler, or the derivative with `deriv`).
+int step_once(const fk_grid &g, const float *in, float *out, const float *D, const Model &m,
+              const Stim *st, int ns, int64_t t, float dt, float rdx, bool deriv,
+              const CUtensorMap &tm_d, MapCache &maps, cudaStream_t stream) {
+    const int64_t plane = g.H * g.pitch;
+    const CUtensorMap *tm_u = nullptr;
+    int rc = maps.get(g, in + 2 * plane, &tm_u);
+    if (rc) return rc;
+    StepArgs a{};
+    a.v = in;
+    a.w = in + plane;
+    a.u = in + 2 * plane;
+    a.D = D;
+    a.vo = out;
+    a.wo = out + plane;
+    a.uo = out + 2 * plane;
+    a.H = (int)g.H;
+    a.W = (int)g.W;
+    a.pitch = (int)g.pitch;
+    a.t = (float)t;
+    a.dt = dt;
+    a.rdx = rdx;
+    a.n_stim = ns;
+    a.m = m;
+    for (int k = 0; k < ns; ++k) a.stim[k] = st[k];
+    a.status = status_ptr();
+    if (!a.status) return FK_ERR_CUDA;
+    cudaError_t e = launch_step(*tm_u, tm_d, a, deriv, stream);
+    return e == cudaSuccess ? FK_OK : FK_ERR_CUDA;
+}
+
+__global__ void fill_state_kernel(float *s, int64_t plane) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (; i < 3 * plane; i += stride) s[i] = i < 2 * plane ? 1.0f : 0.0f;
+}
+
+}  // namespace fk
+
+using namespace fk;
+
+// ---- exported entry points ---------------------------------------------------------------
+extern "C" {
+
+const char *fk_status_string(int s) {
+    switch (s) {
+        case FK_OK: return "ok";
+        case FK_ERR_NULL: return "null pointer";
+        case FK_ERR_SHAPE: return "invalid grid shape (need H, W >= 3 and pitch >= W)";
+        case FK_ERR_ALIGN: return "misaligned buffer (need pitch % 4 == 0 and 16-byte aligned pointers)";
+        case FK_ERR_STIMULI: return "invalid stimuli (too many, or a non-finite or zero-period protocol)";
+        case FK_ERR_ARGUMENT: return "invalid argument";
+        case FK_ERR_CUDA: return "CUDA error";
+        case FK_ERR_TENSORMAP: return "TMA descriptor encoding failed";
+        case FK_ERR_DEVICE: return "device-side barrier timeout";
+        default: return "unknown status";
+    }
+}
+
+int fk_device_status(int reset, int *value) {
+    int *p = status_ptr();
+    if (!p || !value) return !value ? FK_ERR_NULL : FK_ERR_CUDA;
+    if (cudaMemcpy(value, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FK_ERR_CUDA;
+    if (reset && cudaMemset(p, 0, sizeof(int)) != cudaSuccess) return FK_ERR_CUDA;
+    return FK_OK;
+}
+
+int fk_init(fk_grid g, float *state, void *stream) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (!state) return FK_ERR_NULL;
+    fill_state_kernel<<<1024, 256, 0, (cudaStream_t)stream>>>(state, g.H * g.pitch);
+    return cudaGetLastError() == cudaSuccess ? FK_OK : FK_ERR_CUDA;
+}
+
+static int common_checks(const fk_grid &g, const void *a, const void *b, const float *D,
+                         const fk_params *p, double dx) {
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (!a || !b || !D || !p) return FK_ERR_NULL;
+    if (!aligned16(a) || !aligned16(b) || !aligned16(D)) return FK_ERR_ALIGN;
+    if (!(dx > 0.0) || !std::isfinite(dx)) return FK_ERR_ARGUMENT;
+    return FK_OK;
+}
+
+int fk_step(fk_grid g, const float *state, const float *D, const fk_params *p,
+            const fk_stimulus *stimuli, int n_stimuli, int64_t t, double dx, float *dstate,
+            void *stream) {
+    int rc = common_checks(g, state, dstate, D, p, dx);
+    if (rc) return rc;
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    MapCache maps;
+    return step_once(g, state, dstate, D, make_model(*p), st, n_stimuli, t, 0.0f,
+                     1.0f / (float)dx, true, tm_d, maps, (cudaStream_t)stream);
+}
+
+int fk_euler_step(fk_grid g, const float *state, const float *D, const fk_params *p,
+                  const fk_stimulus *stimuli, int n_stimuli, int64_t t, double dt, double dx,
+                  float *state_out, void *stream) {
+    int rc = common_checks(g, state, state_out, D, p, dx);
+    if (rc) return rc;
+    if (!std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    MapCache maps;
+    return step_once(g, state, state_out, D, make_model(*p), st, n_stimuli, t, (float)dt,
+                     1.0f / (float)dx, false, tm_d, maps, (cudaStream_t)stream);
+}
+
+int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, const fk_params *p,
+                     const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1,
+                     double dt, double dx, void *stream) {
+    int rc = common_checks(g, state, scratch, D, p, dx);
+    if (rc) return rc;
+    if (t1 < t0 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    const Model m = make_model(*p);
+    const float rdx = 1.0f / (float)dx;
+    cudaStream_t s = (cudaStream_t)stream;
+    float *bufs[2] = {state, scratch};
+    MapCache maps;
+    for (int64_t t = t0; t < t1; ++t) {
+        const int k = (int)((t - t0) & 1);
+        rc = step_once(g, bufs[k], bufs[k ^ 1], D, m, st, n_stimuli, t, (float)dt, rdx, false,
+                       tm_d, maps, s);
+        if (rc) return rc;
+    }
+    if ((t1 - t0) & 1) {
+        // odd number of steps: the result sits in scratch
+        if (cudaMemcpyAsync(state, scratch, sizeof(float) * 3 * g.H * g.pitch,
+                            cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return FK_ERR_CUDA;
+    }
+    return FK_OK;
+}
+
+int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
+               const fk_params *p, const fk_stimulus *stimuli, int n_stimuli,
+               const int64_t *checkpoints, int n_checkpoints, double dt, double dx, float *out,
+               void *stream) {
+    int rc = common_checks(g, state0, scratch, D, p, dx);
+    if (rc) return rc;
+    if (!out || !checkpoints) return FK_ERR_NULL;
+    if (!aligned16(out)) return FK_ERR_ALIGN;
+    if (n_checkpoints < 1 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    for (int i = 0; i + 1 < n_checkpoints; ++i)
+        if (checkpoints[i + 1] < checkpoints[i]) return FK_ERR_ARGUMENT;
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    const Model m = make_model(*p);
+    const float rdx = 1.0f / (float)dx;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t n_state = 3 * g.H * g.pitch;
+    const float *cur = state0;
+    MapCache maps;
+    for (int i = 0; i + 1 < n_checkpoints; ++i) {
+        float *dst = out + (int64_t)i * n_state;
+        const int64_t a = checkpoints[i], b = checkpoints[i + 1], n = b - a;
+        if (n == 0) {
+            if (cudaMemcpyAsync(dst, cur, sizeof(float) * n_state, cudaMemcpyDeviceToDevice, s) !=
+                cudaSuccess)
+                return FK_ERR_CUDA;
+        }
+        // ping-pong so that the interval's last step lands in dst
+        for (int64_t k = 0; k < n; ++k) {
+            float *o = ((n - 1 - k) & 1) ? scratch : dst;
+            rc = step_once(g, cur, o, D, m, st, n_stimuli, a + k, (float)dt, rdx, false, tm_d,
+                           maps, s);
+            if (rc) return rc;
+            cur = o;
+        }
+        cur = dst;
+    }
+    return FK_OK;
+}
+
+}  // extern "C"

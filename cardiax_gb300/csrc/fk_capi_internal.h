@@ -1,0 +1,20 @@
+// Helpers shared by the C-ABI translation units (not part of the public ABI).
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/cardiax_gb300.h"
+#include "fk_math.cuh"
+
+namespace fk {
+
+int *status_ptr();
+int make_plane_map(CUtensorMap *map, const float *plane, int64_t H, int64_t W, int64_t pitch,
+                   int box_w, int box_h);
+int check_grid(const fk_grid &g);
+Model make_model(const fk_params &p);
+int make_stims(const fk_stimulus *s, int n, const fk_grid &g, Stim *out);
+
+}  // namespace fk

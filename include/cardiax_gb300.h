@@ -1,0 +1,108 @@
+/*
+ * cardiax_gb300 -- C ABI of the GB300 Fenton-Karma stepper.
+ *
+ * Plain pointers and sizes only.  Every device pointer is a CUDA device address; `stream` is a
+ * cudaStream_t (NULL = the legacy default stream).  No entry point allocates device memory:
+ * callers pass every buffer, including the ping-pong scratch state.
+ *
+ * Layout
+ *   A grid is H rows x W columns of float32 with a row pitch of `pitch` elements
+ *   (pitch >= W, pitch % 4 == 0, base addresses 16-byte aligned).  A state is three such planes
+ *   back to back -- v, w, u, the field order of the reference's State (cardiax/solve.py:12-15) --
+ *   so plane p starts at state + p * H * pitch.  The diffusivity map and dense stimulus fields
+ *   are single planes with the same pitch.
+ *
+ * Time
+ *   Steps are integers; the stimulus protocol is evaluated on the float32 step index exactly as
+ *   the reference's loop does (cardiax/solve.py:92-100, 262-267).
+ *
+ * Errors
+ *   Every entry point returns FK_OK (0) or a positive fk_status code; fk_status_string() names
+ *   it.  Launch errors are reported synchronously; device-side barrier timeouts set a sticky
+ *   word read by fk_device_status().
+ */
+#ifndef CARDIAX_GB300_H
+#define CARDIAX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    FK_OK = 0,
+    FK_ERR_NULL = 1,       /* a required pointer is NULL                          */
+    FK_ERR_SHAPE = 2,      /* H or W < 3, pitch < W, or sizes out of range         */
+    FK_ERR_ALIGN = 3,      /* pitch % 4 != 0 or a pointer is not 16-byte aligned   */
+    FK_ERR_STIMULI = 4,    /* too many stimuli or an invalid protocol              */
+    FK_ERR_ARGUMENT = 5,   /* any other invalid argument (dx <= 0, t1 < t0, ...)   */
+    FK_ERR_CUDA = 6,       /* a CUDA call failed                                   */
+    FK_ERR_TENSORMAP = 7,  /* the TMA descriptor could not be encoded              */
+    FK_ERR_DEVICE = 8      /* a kernel reported a barrier timeout                  */
+} fk_status;
+
+/* The 14 Fenton-Karma parameters in the reference's field order (cardiax/params.py:4-18). */
+typedef struct {
+    float tau_v_plus, tau_v1_minus, tau_v2_minus, tau_w_plus, tau_w_minus;
+    float tau_d, tau_0, tau_r, tau_si, k, V_csi, V_c, V_v, Cm;
+} fk_params;
+
+/* One stimulus (cardiax/stimulus.py:13-21).  Protocol values are in steps.  The field is
+ * either dense (`field` != NULL, one plane with the grid's pitch) or, when `field` is NULL, the
+ * rectangle [r0, r1) x [c0, c1) of value `amplitude` and zero elsewhere.  Where active stimuli
+ * overlap, the later one in the list wins; a zero field value leaves the ionic current. */
+typedef struct {
+    double start, duration, period;
+    const float *field;
+    int32_t r0, r1, c0, c1;
+    float amplitude;
+} fk_stimulus;
+
+#define FK_MAX_STIMULI 8
+
+typedef struct {
+    int64_t H, W, pitch;
+} fk_grid;
+
+/* Name of a status code. */
+const char *fk_status_string(int status);
+
+/* Reads (and with reset != 0 clears) the device error word of the current device. */
+int fk_device_status(int reset, int *value);
+
+/* init (cardiax/solve.py:18-23): v = w = 1, u = 0 on the three planes of `state`. */
+int fk_init(fk_grid g, float *state, void *stream);
+
+/* step (cardiax/solve.py:26-65): the time derivative (dv, dw, du) of `state` at step `t`,
+ * written to `dstate` (a separate state buffer). */
+int fk_step(fk_grid g, const float *state, const float *D, const fk_params *p,
+            const fk_stimulus *stimuli, int n_stimuli, int64_t t, double dx, float *dstate,
+            void *stream);
+
+/* step_euler (cardiax/solve.py:68-70): one explicit Euler step from `state` at step `t` into
+ * `state_out` (a separate buffer). */
+int fk_euler_step(fk_grid g, const float *state, const float *D, const fk_params *p,
+                  const fk_stimulus *stimuli, int n_stimuli, int64_t t, double dt, double dx,
+                  float *state_out, void *stream);
+
+/* _forward_euler (cardiax/solve.py:92-100): steps t0 .. t1-1 applied to `state` in place;
+ * `scratch` is a second state buffer of the same size. */
+int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, const fk_params *p,
+                     const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1,
+                     double dt, double dx, void *stream);
+
+/* forward (cardiax/solve.py:168-222): for i in 0 .. n_checkpoints-2, advances from
+ * checkpoints[i] to checkpoints[i+1] and writes that state to out + i * 3 * H * pitch.
+ * `state0` is only read; `scratch` is one state buffer.  Checkpoints must be non-decreasing. */
+int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
+               const fk_params *p, const fk_stimulus *stimuli, int n_stimuli,
+               const int64_t *checkpoints, int n_checkpoints, double dt, double dx, float *out,
+               void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CARDIAX_GB300_H */

@@ -1,0 +1,66 @@
+"""The C-ABI library builds, loads and exports every symbol of include/*.h; argument checks
+that fail before any device work return their status codes (no GPU needed)."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(fk_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    from cardiax_gb300 import _native as N
+    N.lib()
+    lib = ctypes.CDLL(N.lib_path())
+    declared = _declared()
+    assert len(declared) >= 7
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(N.exported_symbols()) <= set(declared)
+
+
+def test_status_strings():
+    from cardiax_gb300 import _native as N
+    L = N.lib()
+    for code in range(0, 9):
+        assert L.fk_status_string(code)
+    assert L.fk_status_string(2).decode().startswith("invalid grid")
+
+
+@pytest.mark.parametrize("H,W,pitch,expect", [(2, 8, 8, 2), (8, 2, 8, 2), (8, 8, 6, 2),
+                                              (8, 6, 6, 3)])
+def test_shape_checks(H, W, pitch, expect):
+    from cardiax_gb300 import _native as N
+    L = N.lib()
+    p = N.Params(*[1.0] * 14)
+    s = (N.Stimulus * 1)()
+    ck = (ctypes.c_int64 * 2)(0, 1)
+    rc = L.fk_forward(N.Grid(H, W, pitch), 16, 32, 48, ctypes.byref(p), s, 0, ck, 2, 0.01, 0.01,
+                      64, None)
+    assert rc == expect
+
+
+def test_null_and_argument_checks():
+    from cardiax_gb300 import _native as N
+    L = N.lib()
+    p = N.Params(*[1.0] * 14)
+    s = (N.Stimulus * 9)()
+    g = N.Grid(8, 8, 8)
+    assert L.fk_forward_euler(g, None, 32, 48, ctypes.byref(p), s, 0, 0, 1, 0.01, 0.01, None) == 1
+    assert L.fk_forward_euler(g, 16, 32, 48, ctypes.byref(p), s, 0, 0, 1, 0.01, -1.0, None) == 5
+    assert L.fk_forward_euler(g, 16, 32, 48, ctypes.byref(p), s, 0, 5, 1, 0.01, 0.01, None) == 5
+    assert L.fk_forward_euler(g, 18, 32, 48, ctypes.byref(p), s, 0, 0, 1, 0.01, 0.01, None) == 3
+    assert L.fk_forward_euler(g, 16, 32, 48, ctypes.byref(p), s, 9, 0, 1, 0.01, 0.01, None) == 4
+    ck = (ctypes.c_int64 * 3)(0, 5, 3)
+    assert L.fk_forward(g, 16, 32, 48, ctypes.byref(p), s, 0, ck, 3, 0.01, 0.01, 64, None) == 5

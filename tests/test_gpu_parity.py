@@ -1,0 +1,215 @@
+"""GPU parity: the CUDA stepper (through the C ABI) against the reference's golden vectors and
+the CPU oracle.
+
+Tolerances (float32, stated per test): the kernels multiply by float32 reciprocals and use
+fused multiply-adds where the reference divides and rounds each product, so single-step
+derivatives differ from the reference in the last bits; over 1000 steps of a travelling wave
+these differences grow to ~1e-5 (the oracle's own float32-vs-float64 gap is the same size), and
+the bar is max|du| <= 1e-4.
+"""
+import numpy as np
+import pytest
+import torch
+
+import fk_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+P3 = (3.33, 19.6, 1250, 870, 41, 0.25, 12.5, 33.33, 29, 10, 0.85, 0.13, 0.04, 1)
+TOL_U_1000 = 1e-4   # pointwise max|du| after 1000 steps (spec bar)
+
+
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def test_step_derivative_golden(golden):
+    """fk_step vs the reference's step on small grids with two stimuli."""
+    _gpu()
+    from cardiax_gb300 import solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    s = golden("step.npz")
+    for k in range(4):
+        st = solve.State(*(torch.as_tensor(s[f"{n}_{k}"]) for n in "vwu"))
+        stims = [Stimulus(Protocol(0, 2, 1e9), s[f"f1_{k}"]), Stimulus(Protocol(1, 3, 7), s[f"f2_{k}"])]
+        for t in (0, 1, 5):
+            d = solve.step(st, t, P3, s[f"D_{k}"], stims, 0.01)
+            for name, arr in zip(("dv", "dw", "du"), d):
+                ref = s[f"{name}_{k}_{t}"]
+                err = np.abs(_np(arr) - ref).max() / max(1.0, np.abs(ref).max())
+                assert err <= (1e-4 if name == "du" else 1e-6), (name, k, t, err)
+
+
+@pytest.mark.parametrize("tag,dtype", [("f32", np.float32)])
+def test_forward_small_golden(golden, tag, dtype):
+    """200 steps on 32x40 with a smooth D and two stimuli vs the reference (f32) and the
+    reference with x64 (reported)."""
+    _gpu()
+    from cardiax_gb300 import solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    g = golden("forward_small.npz")
+    shp = g["D"].shape
+    stims = [Stimulus(Protocol(0, 2, 1e9), g["f1"]), Stimulus(Protocol(60, 3, 1e9), g["f2"])]
+    res = solve._forward_euler(solve.init(shp), 0, 200, P3, g["D"], stims, 0.01, 0.01)
+    for name, arr in zip("vwu", res):
+        e32 = np.abs(_np(arr) - g[f"{name}_f32"]).max()
+        e64 = np.abs(_np(arr) - g[f"{name}_f64"]).max()
+        print(f"forward_small {name}: |gpu-ref32| {e32:.3g}  |gpu-ref64| {e64:.3g}")
+        assert e32 <= 2e-5
+
+
+@pytest.mark.parametrize("tag", ["plain", "excite"])
+def test_config0_1000_steps_golden(golden, tag):
+    """The 128x128 configuration, 1000 steps, checkpoints every 100: max|du| <= 1e-4 at every
+    checkpoint vs the reference."""
+    _gpu()
+    from cardiax_gb300 import solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    g = golden("config0.npz")
+    proto = Protocol(0, 200, 1e9) if tag == "plain" else Protocol(0, 2, 1e9)
+    D = np.full((128, 128), 0.001, np.float32)
+    states = solve.forward(solve.init((128, 128)), list(range(0, 1001, 100)), P3, D,
+                           [Stimulus(proto, g[f"{tag}_field"])], 0.01, 0.01)
+    assert len(states) == 10
+    worst = 0.0
+    for i, s in enumerate(states):
+        e = np.abs(_np(s.u) - g[f"{tag}_u_{(i + 1) * 100}"]).max()
+        worst = max(worst, e)
+        assert e <= TOL_U_1000, (tag, (i + 1) * 100, e)
+    assert np.abs(_np(states[-1].v) - g[f"{tag}_v_final"]).max() <= TOL_U_1000
+    assert np.abs(_np(states[-1].w) - g[f"{tag}_w_final"]).max() <= TOL_U_1000
+    print(f"config0 {tag}: max|du| over checkpoints {worst:.3g}")
+    if tag == "excite":
+        assert float(states[-1].u.max()) > 0.9  # the wave did propagate
+
+
+def _smooth(rng, shape, lo, hi):
+    H, W = shape
+    i, j = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    f = np.zeros(shape)
+    for _ in range(3):
+        ci, cj, s = rng.uniform(0, H), rng.uniform(0, W), rng.uniform(0.2, 0.5) * max(H, W)
+        f += rng.uniform(-1, 1) * np.exp(-((i - ci) ** 2 + (j - cj) ** 2) / (2 * s * s))
+    f = (f - f.min()) / (f.max() - f.min() + 1e-12)
+    return (lo + (hi - lo) * f).astype(np.float32)
+
+
+@pytest.mark.parametrize("shape", [(3, 3), (3, 5), (5, 3), (4, 7), (9, 13), (33, 37), (7, 130),
+                                   (130, 7), (64, 64), (100, 260)])
+def test_edge_shapes_vs_oracle(shape):
+    """Grids that exercise every boundary formula, widths that are not multiples of 4 and tiles
+    that are partly outside the grid: derivative and 60 Euler steps vs the oracle."""
+    _gpu()
+    from cardiax_gb300 import solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    rng = np.random.default_rng(sum(shape))
+    st = tuple(_smooth(rng, shape, 0.0, 1.0) for _ in range(3))
+    D = _smooth(rng, shape, 3e-4, 1e-3)
+    f = np.zeros(shape, np.float32)
+    f[:, : max(1, shape[1] // 4)] = 15.0
+    stims_o = [O.OStim(0, 2, 1e9, f)]
+    stims_g = [Stimulus(Protocol(0, 2, 1e9), f)]
+    d_ref = O.derivative(O.OState(*st), np.float32(0), P3, D, stims_o, 0.01)
+    d_gpu = solve.step(solve.State(*map(torch.as_tensor, st)), 0, P3, D, stims_g, 0.01)
+    for a, b in zip(d_gpu, d_ref):
+        assert np.abs(_np(a) - b).max() / max(1.0, np.abs(b).max()) <= 1e-4
+    ref = O.forward_euler(O.OState(*st), 0, 60, P3, D, stims_o, 0.01, 0.01)
+    got = solve._forward_euler(solve.State(*map(torch.as_tensor, st)), 0, 60, P3, D, stims_g,
+                               0.01, 0.01)
+    for a, b in zip(got, ref):
+        assert np.all(np.isfinite(_np(a)))
+        assert np.abs(_np(a) - b).max() <= 1e-4, shape
+
+
+def test_rect_and_dense_stimuli_agree_bitwise():
+    """A constant rectangle runs as a descriptor, a field with two values as a dense plane;
+    equal fields must give identical bits, and overlapping stimuli follow list order."""
+    _gpu()
+    from cardiax_gb300 import solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    shp = (48, 72)
+    r1 = np.zeros(shp, np.float32)
+    r1[10:20, 30:50] = 8.0
+    r2 = np.zeros(shp, np.float32)
+    r2[30:40, 5:9] = 8.0
+    dense = r1 + r2  # not a single rectangle -> dense plane
+    D = np.full(shp, 8e-4, np.float32)
+    a = solve._forward_euler(solve.init(shp), 0, 30, P3, D,
+                             [Stimulus(Protocol(0, 5, 10), r1), Stimulus(Protocol(0, 5, 10), r2)],
+                             0.01, 0.01)
+    b = solve._forward_euler(solve.init(shp), 0, 30, P3, D, [Stimulus(Protocol(0, 5, 10), dense)],
+                             0.01, 0.01)
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+    from cardiax_gb300.tissue import analyse_field
+    assert analyse_field(torch.as_tensor(dense).cuda())[0] == "dense"
+    assert analyse_field(torch.as_tensor(r1).cuda())[0] == "rect"
+    # overlap: later stimulus wins where both are non-zero
+    s1 = np.zeros(shp, np.float32); s1[:, :10] = 5.0
+    s2 = np.zeros(shp, np.float32); s2[:, 5:15] = 9.0
+    stims = [Stimulus(Protocol(0, 2, 1e9), s1), Stimulus(Protocol(0, 2, 1e9), s2)]
+    d = solve.step(solve.init(shp), 0, P3, D, stims, 0.01)
+    ref = O.derivative(O.init(shp), np.float32(0), P3, D, [O.OStim(0, 2, 1e9, s1), O.OStim(0, 2, 1e9, s2)], 0.01)
+    assert np.abs(_np(d.u) - ref.u).max() <= 1e-4
+
+
+def test_forward_is_deterministic_and_matches_stepwise():
+    _gpu()
+    from cardiax_gb300 import solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus, linear, Direction
+    shp = (96, 160)
+    D = np.full(shp, 1e-3, np.float32)
+    stims = [linear(shp, Direction.WEST, 0.05, 20.0, Protocol(0, 2, 1e9))]
+    a = solve.forward(solve.init(shp), [0, 7, 20, 20, 45], P3, D, stims, 0.01, 0.01)
+    b = solve.forward(solve.init(shp), [0, 7, 20, 20, 45], P3, D, stims, 0.01, 0.01)
+    assert len(a) == 4
+    for x, y in zip(a, b):
+        for p, q in zip(x, y):
+            assert torch.equal(p, q)
+    assert torch.equal(a[1].u, a[2].u)  # repeated checkpoint
+    s = solve.init(shp)
+    for t in range(45):
+        s = solve.step_euler(s, t, P3, D, stims, 0.01, 0.01)
+    for p, q in zip(a[-1], s):
+        assert torch.equal(p, q)
+
+
+def test_too_many_stimuli_rejected():
+    _gpu()
+    from cardiax_gb300 import solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    shp = (16, 16)
+    stims = []
+    for k in range(9):
+        f = np.zeros(shp, np.float32)
+        f[k, :] = 1.0
+        stims.append(Stimulus(Protocol(0, 2, 5), f))
+    with pytest.raises(ValueError):
+        solve._forward_euler(solve.init(shp), 0, 3, P3, np.full(shp, 1e-3, np.float32), stims, 0.01, 0.01)
+
+
+def test_full_size_2048_vs_c_oracle():
+    """2048x2048 with a noisy D and a periodic left-edge stimulus (the roofline configuration),
+    30 steps through the GPU vs the C oracle on the host."""
+    _gpu()
+    import fk_oracle_c as C
+    from cardiax_gb300 import solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    H = W = 2048
+    rng = np.random.default_rng(3)
+    D = np.clip(0.001 * (1 + 0.05 * rng.standard_normal((H, W))), 0, None).astype(np.float32)
+    f = np.zeros((H, W), np.float32)
+    f[:, :5] = 20.0
+    st0 = O.init((H, W))
+    st0.u[:, :] = _smooth(rng, (H, W), 0.0, 0.3)
+    ref = C.forward_euler(st0, 0, 30, P3, D, [(0, 200, 20000, f)], 0.01, 0.01,
+                          threads=C.max_threads())
+    got = solve._forward_euler(solve.State(*map(torch.as_tensor, st0)), 0, 30, P3, D,
+                               [Stimulus(Protocol(0, 200, 20000), f)], 0.01, 0.01)
+    for a, b in zip(got, ref):
+        assert np.abs(_np(a) - b).max() <= 1e-4

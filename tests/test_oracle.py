@@ -1,0 +1,100 @@
+"""The CPU oracle against the reference's golden vectors (no GPU).
+
+The fixtures were produced by running the reference's own solve.py (tests/golden/make_golden.py);
+the oracle must reproduce them bit for bit in float32 (same evaluation order) and in float64.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import fk_oracle as O
+from conftest import GOLDEN
+
+P3 = (3.33, 19.6, 1250, 870, 41, 0.25, 12.5, 33.33, 29, 10, 0.85, 0.13, 0.04, 1)
+
+
+def test_stimulus_schedule_known_answer():
+    # tests/macro/stimulate_test.py:16-18 of the reference
+    A = {0, 1, 50, 51, 100, 101, 150, 151, 200, 201, 250, 251}
+    B = {10, 11, 60, 61, 110, 111, 160, 161, 210, 211, 260, 261}
+    C = {30, 31}
+    for proto, want in (((0, 2, 50), A), ((10, 2, 50), B), ((30, 2, 1000000), C)):
+        got = {t for t in range(300) if O.stimulus_active(t, *proto)}
+        assert got == want
+
+
+def test_stimulus_schedule_golden():
+    sched = json.load(open(os.path.join(GOLDEN, "stimulus_schedule.json")))
+    for name, rec in sched.items():
+        got = [t for t in range(300) if O.stimulus_active(t, *rec["protocol"])]
+        assert got == rec["active"], name
+
+
+def test_gradient_golden(golden):
+    g = golden("gradient.npz")
+    for k in range(4):
+        a = g[f"in{k}"]
+        np.testing.assert_array_equal(O.gradient(a, 0), g[f"ax0_{k}"])
+        np.testing.assert_array_equal(O.gradient(a, 1), g[f"ax1_{k}"])
+
+
+def test_step_golden(golden):
+    s = golden("step.npz")
+    for k in range(4):
+        st = O.OState(s[f"v_{k}"], s[f"w_{k}"], s[f"u_{k}"])
+        stims = [O.OStim(0, 2, 1e9, s[f"f1_{k}"]), O.OStim(1, 3, 7, s[f"f2_{k}"])]
+        for t in (0, 1, 5):
+            d = O.derivative(st, np.float32(t), P3, s[f"D_{k}"], stims, 0.01)
+            for name, arr in zip(("dv", "dw", "du"), d):
+                np.testing.assert_array_equal(arr, s[f"{name}_{k}_{t}"], err_msg=f"{name} {k} {t}")
+
+
+@pytest.mark.parametrize("tag,dtype", [("f32", np.float32), ("f64", np.float64)])
+def test_forward_small_golden(golden, tag, dtype):
+    g = golden("forward_small.npz")
+    shp = g["D"].shape
+    stims = [O.OStim(0, 2, 1e9, g["f1"].astype(dtype)), O.OStim(60, 3, 1e9, g["f2"].astype(dtype))]
+    res = O.forward_euler(O.init(shp, dtype), 0, 200, P3, g["D"].astype(dtype), stims, 0.01, 0.01)
+    for name, arr in zip("vwu", res):
+        np.testing.assert_array_equal(arr, g[f"{name}_{tag}"])
+
+
+def test_config0_golden(golden):
+    g = golden("config0.npz")
+    for tag in ("plain", "excite"):
+        field = g[f"{tag}_field"]
+        proto = (0, 200, 1e9) if tag == "plain" else (0, 2, 1e9)
+        np.testing.assert_array_equal(field, O.linear_field((128, 128), 3, 5 / 128,
+                                                            1.0 if tag == "plain" else 20.0))
+        st = O.init((128, 128))
+        D = np.full((128, 128), 0.001, np.float32)
+        states = O.forward(st, list(range(0, 1001, 100))[:4], P3, D, [O.OStim(*proto, field)],
+                           0.01, 0.01)
+        for i, s in enumerate(states):
+            np.testing.assert_array_equal(s.u, g[f"{tag}_u_{(i + 1) * 100}"])
+
+
+def test_c_oracle_matches_numpy_oracle():
+    """The C restatement agrees with the NumPy one up to libm-vs-NumPy tanh rounding."""
+    import fk_oracle_c as C
+    C.build()
+    g = np.load(os.path.join(GOLDEN, "forward_small.npz"))
+    shp = g["D"].shape
+    for dtype, tol in ((np.float32, 5e-5), (np.float64, 1e-12)):
+        stims = [(0, 2, 1e9, g["f1"].astype(dtype)), (60, 3, 1e9, g["f2"].astype(dtype))]
+        v, w, u = C.forward_euler(O.init(shp, dtype), 0, 200, P3, g["D"].astype(dtype), stims,
+                                  0.01, 0.01, threads=2)
+        ref = "f32" if dtype == np.float32 else "f64"
+        assert np.abs(u - g[f"u_{ref}"]).max() <= tol
+        assert np.abs(v - g[f"v_{ref}"]).max() <= tol
+        assert np.abs(w - g[f"w_{ref}"]).max() <= tol
+
+
+def test_params_golden():
+    from cardiax_gb300 import params as Pm
+    rec = json.load(open(os.path.join(GOLDEN, "params.json")))
+    assert list(Pm.Params._fields) == rec["fields"]
+    for name, vals in rec["sets"].items():
+        assert [float(x) for x in getattr(Pm, name)] == vals, name
