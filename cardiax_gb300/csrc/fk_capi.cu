@@ -150,7 +150,7 @@ struct MapCache {
 // One step from `in` to `out` (Euler, or the derivative with `deriv`).
 int step_once(const fk_grid &g, const float *in, float *out, const float *D, const Model &m,
               const Stim *st, int ns, int64_t t, float dt, float rdx, bool deriv,
-              const CUtensorMap &tm_d, MapCache &maps, cudaStream_t stream) {
+              const CUtensorMap &tm_d, MapCache &maps, int *status, cudaStream_t stream) {
     const int64_t plane = g.H * g.pitch;
     const CUtensorMap *tm_u = nullptr;
     int rc = maps.get(g, in + 2 * plane, &tm_u);
@@ -172,8 +172,7 @@ int step_once(const fk_grid &g, const float *in, float *out, const float *D, con
     a.n_stim = ns;
     a.m = m;
     for (int k = 0; k < ns; ++k) a.stim[k] = st[k];
-    a.status = status_ptr();
-    if (!a.status) return FK_ERR_CUDA;
+    a.status = status;
     cudaError_t e = launch_step(*tm_u, tm_d, a, deriv, stream);
     return e == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
@@ -241,9 +240,11 @@ int fk_step(fk_grid g, const float *state, const float *D, const fk_params *p,
     if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
     MapCache maps;
     return step_once(g, state, dstate, D, make_model(*p), st, n_stimuli, t, 0.0f,
-                     1.0f / (float)dx, true, tm_d, maps, (cudaStream_t)stream);
+                     1.0f / (float)dx, true, tm_d, maps, status, (cudaStream_t)stream);
 }
 
 int fk_euler_step(fk_grid g, const float *state, const float *D, const fk_params *p,
@@ -256,9 +257,11 @@ int fk_euler_step(fk_grid g, const float *state, const float *D, const fk_params
     if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
     MapCache maps;
     return step_once(g, state, state_out, D, make_model(*p), st, n_stimuli, t, (float)dt,
-                     1.0f / (float)dx, false, tm_d, maps, (cudaStream_t)stream);
+                     1.0f / (float)dx, false, tm_d, maps, status, (cudaStream_t)stream);
 }
 
 int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, const fk_params *p,
@@ -271,6 +274,8 @@ int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, co
     if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
     const Model m = make_model(*p);
     const float rdx = 1.0f / (float)dx;
     cudaStream_t s = (cudaStream_t)stream;
@@ -279,7 +284,7 @@ int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, co
     for (int64_t t = t0; t < t1; ++t) {
         const int k = (int)((t - t0) & 1);
         rc = step_once(g, bufs[k], bufs[k ^ 1], D, m, st, n_stimuli, t, (float)dt, rdx, false,
-                       tm_d, maps, s);
+                       tm_d, maps, status, s);
         if (rc) return rc;
     }
     if ((t1 - t0) & 1) {
@@ -306,6 +311,8 @@ int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
     if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
     const Model m = make_model(*p);
     const float rdx = 1.0f / (float)dx;
     cudaStream_t s = (cudaStream_t)stream;
@@ -324,7 +331,7 @@ int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
         for (int64_t k = 0; k < n; ++k) {
             float *o = ((n - 1 - k) & 1) ? scratch : dst;
             rc = step_once(g, cur, o, D, m, st, n_stimuli, a + k, (float)dt, rdx, false, tm_d,
-                           maps, s);
+                           maps, status, s);
             if (rc) return rc;
             cur = o;
         }

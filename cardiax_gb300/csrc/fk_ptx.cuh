@@ -31,21 +31,29 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity), "r"(1000000u)
+        : "r"(smem_addr(bar)), "r"(parity)
         : "memory");
     return ok != 0;
 }
 
-// Waits for the phase with the given parity; gives up after `max_tries` try_wait rounds
-// (each round suspends for at most ~1 ms), so a lost transfer ends as an error, not a hang.
+__device__ __forceinline__ uint64_t global_timer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the phase with the given parity; gives up after `limit_ns` of wall time so that a
+// lost transfer ends as an error status instead of a hang.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
-                                                  uint32_t max_tries = 2000u) {
-    for (uint32_t i = 0; i < max_tries; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
+                                                  uint64_t limit_ns = 1000000000ull) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_timer_ns();
+    while (!mbar_try_wait(bar, parity))
+        if (global_timer_ns() - t0 > limit_ns) return false;
+    return true;
 }
 
 // 2-D tiled TMA load of box (x = inner coordinate, y = outer) into shared memory, completing

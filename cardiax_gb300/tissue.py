@@ -67,35 +67,22 @@ def params_struct(params) -> N.Params:
     return N.Params(*vals)
 
 
-_RECT_CACHE: dict = {}
-
-
 def analyse_field(field: torch.Tensor):
     """Classifies a stimulus field: ``("empty",)`` (all zero), ``("rect", r0, r1, c0, c1, a)``
-    (a constant ``a`` on a rectangle, zero elsewhere) or ``("dense",)``."""
-    key = (field.data_ptr(), field._version, tuple(field.shape), tuple(field.stride()),
-           str(field.device))
-    hit = _RECT_CACHE.get(key)
-    if hit is not None:
-        return hit
+    (a constant ``a`` on a rectangle, zero elsewhere) or ``("dense",)``.  Runs a few reductions
+    on the device and one synchronisation (set-up cost, once per tissue)."""
     nz = field != 0
     rows = torch.nonzero(nz.any(1)).flatten()
     if rows.numel() == 0:
-        res = ("empty",)
-    else:
-        cols = torch.nonzero(nz.any(0)).flatten()
-        r0, r1 = int(rows[0]), int(rows[-1]) + 1
-        c0, c1 = int(cols[0]), int(cols[-1]) + 1
-        box = field[r0:r1, c0:c1]
-        a = box[0, 0]
-        if bool((box == a).all()):
-            res = ("rect", r0, r1, c0, c1, float(a))
-        else:
-            res = ("dense",)
-    if len(_RECT_CACHE) > 256:
-        _RECT_CACHE.clear()
-    _RECT_CACHE[key] = res
-    return res
+        return ("empty",)
+    cols = torch.nonzero(nz.any(0)).flatten()
+    r0, r1 = int(rows[0]), int(rows[-1]) + 1
+    c0, c1 = int(cols[0]), int(cols[-1]) + 1
+    box = field[r0:r1, c0:c1]
+    a = box[0, 0]
+    if bool((box == a).all()):
+        return ("rect", r0, r1, c0, c1, float(a))
+    return ("dense",)
 
 
 def stimulus_table(stimuli: Sequence, H: int, W: int, pitch: int, device):
