@@ -40,6 +40,11 @@ class Stimulus(ctypes.Structure):
                 ("c1", ctypes.c_int32), ("amplitude", ctypes.c_float)]
 
 
+class Activation(ctypes.Structure):
+    _fields_ = [("first", ctypes.c_void_p), ("last", ctypes.c_void_p), ("count", ctypes.c_void_p),
+                ("threshold", ctypes.c_float)]
+
+
 _lib = None
 _lock = threading.Lock()
 _P = ctypes.c_void_p
@@ -59,6 +64,9 @@ _SIGNATURES = {
                          _I64, _I64, _D, _D, _P],
     "fk_forward": [Grid, _P, _P, _P, ctypes.POINTER(Params), ctypes.POINTER(Stimulus), _INT,
                    ctypes.POINTER(_I64), _INT, _D, _D, _P, _P],
+    "fk_forward_euler_tracked": [Grid, _P, _P, _P, ctypes.POINTER(Params),
+                                 ctypes.POINTER(Stimulus), _INT, _I64, _I64, _D, _D,
+                                 ctypes.POINTER(Activation), _P],
 }
 
 

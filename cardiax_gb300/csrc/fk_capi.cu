@@ -5,6 +5,7 @@
 //   fk_step           cardiax/solve.py:26-65   step (time derivative)
 //   fk_euler_step     cardiax/solve.py:68-70   step_euler
 //   fk_forward_euler  cardiax/solve.py:92-100  _forward_euler
+//   fk_forward_euler_tracked  the same, with activation-time maps (no reference counterpart)
 //   fk_forward        cardiax/solve.py:168-222 forward (Euler integrator)
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -126,23 +127,31 @@ int make_stims(const fk_stimulus *s, int n, const fk_grid &g, Stim *out) {
     return FK_OK;
 }
 
-// Tensor maps of the u planes seen by one call (the ping-pong buffers and checkpoint slots).
+// TMA descriptors of the state buffers seen by one call (the ping-pong buffers and checkpoint
+// slots): u with its halo box, v and w with the plain tile box.
 struct MapCache {
     const float *ptr[4] = {nullptr, nullptr, nullptr, nullptr};
-    CUtensorMap map[4];
+    CUtensorMap u[4], v[4], w[4];
     int next = 0;
-    int get(const fk_grid &g, const float *u, const CUtensorMap **out) {
+    int get(const fk_grid &g, const float *state, StepMaps &out) {
+        const int64_t plane = g.H * g.pitch;
+        int k = -1;
         for (int i = 0; i < 4; ++i)
-            if (ptr[i] == u) {
-                *out = &map[i];
-                return FK_OK;
-            }
-        const int k = next;
-        next = (next + 1) & 3;
-        int rc = make_plane_map(&map[k], u, g.H, g.W, g.pitch, SU_W, SU_H);
-        if (rc) return rc;
-        ptr[k] = u;
-        *out = &map[k];
+            if (ptr[i] == state) k = i;
+        if (k < 0) {
+            k = next;
+            next = (next + 1) & 3;
+            int rc;
+            ptr[k] = nullptr;
+            if ((rc = make_plane_map(&u[k], state + 2 * plane, g.H, g.W, g.pitch, SW, SU_H)) ||
+                (rc = make_plane_map(&v[k], state, g.H, g.W, g.pitch, TX, TY)) ||
+                (rc = make_plane_map(&w[k], state + plane, g.H, g.W, g.pitch, TX, TY)))
+                return rc;
+            ptr[k] = state;
+        }
+        out.u = u[k];
+        out.v = v[k];
+        out.w = w[k];
         return FK_OK;
     }
 };
@@ -150,11 +159,13 @@ struct MapCache {
 // One step from `in` to `out` (Euler, or the derivative with `deriv`).
 int step_once(const fk_grid &g, const float *in, float *out, const float *D, const Model &m,
               const Stim *st, int ns, int64_t t, float dt, float rdx, bool deriv,
-              const CUtensorMap &tm_d, MapCache &maps, int *status, cudaStream_t stream) {
+              const CUtensorMap &tm_d, MapCache &maps, int *status, cudaStream_t stream,
+              const fk_activation *act = nullptr) {
     const int64_t plane = g.H * g.pitch;
-    const CUtensorMap *tm_u = nullptr;
-    int rc = maps.get(g, in + 2 * plane, &tm_u);
+    StepMaps sm;
+    int rc = maps.get(g, in, sm);
     if (rc) return rc;
+    sm.d = tm_d;
     StepArgs a{};
     a.v = in;
     a.w = in + plane;
@@ -173,7 +184,13 @@ int step_once(const fk_grid &g, const float *in, float *out, const float *D, con
     a.m = m;
     for (int k = 0; k < ns; ++k) a.stim[k] = st[k];
     a.status = status;
-    cudaError_t e = launch_step(*tm_u, tm_d, a, deriv, stream);
+    if (act && !deriv) {
+        a.act_first = act->first;
+        a.act_last = act->last;
+        a.act_count = act->count;
+        a.act_threshold = act->threshold;
+    }
+    cudaError_t e = launch_step(sm, a, deriv, stream);
     return e == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
 
@@ -239,7 +256,7 @@ int fk_step(fk_grid g, const float *state, const float *D, const fk_params *p,
     Stim st[kMaxStim];
     if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
     CUtensorMap tm_d;
-    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
     if (!status) return FK_ERR_CUDA;
     MapCache maps;
@@ -256,7 +273,7 @@ int fk_euler_step(fk_grid g, const float *state, const float *D, const fk_params
     Stim st[kMaxStim];
     if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
     CUtensorMap tm_d;
-    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
     if (!status) return FK_ERR_CUDA;
     MapCache maps;
@@ -264,16 +281,21 @@ int fk_euler_step(fk_grid g, const float *state, const float *D, const fk_params
                      1.0f / (float)dx, false, tm_d, maps, status, (cudaStream_t)stream);
 }
 
-int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, const fk_params *p,
-                     const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1,
-                     double dt, double dx, void *stream) {
+int fk_forward_euler_tracked(fk_grid g, float *state, float *scratch, const float *D,
+                             const fk_params *p, const fk_stimulus *stimuli, int n_stimuli,
+                             int64_t t0, int64_t t1, double dt, double dx,
+                             const fk_activation *act, void *stream) {
     int rc = common_checks(g, state, scratch, D, p, dx);
     if (rc) return rc;
     if (t1 < t0 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    if (act) {
+        if (!act->first || !act->last || !act->count) return FK_ERR_NULL;
+        if (!std::isfinite(act->threshold)) return FK_ERR_ARGUMENT;
+    }
     Stim st[kMaxStim];
     if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
     CUtensorMap tm_d;
-    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
     if (!status) return FK_ERR_CUDA;
     const Model m = make_model(*p);
@@ -284,7 +306,7 @@ int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, co
     for (int64_t t = t0; t < t1; ++t) {
         const int k = (int)((t - t0) & 1);
         rc = step_once(g, bufs[k], bufs[k ^ 1], D, m, st, n_stimuli, t, (float)dt, rdx, false,
-                       tm_d, maps, status, s);
+                       tm_d, maps, status, s, act);
         if (rc) return rc;
     }
     if ((t1 - t0) & 1) {
@@ -294,6 +316,13 @@ int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, co
             return FK_ERR_CUDA;
     }
     return FK_OK;
+}
+
+int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, const fk_params *p,
+                     const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1,
+                     double dt, double dx, void *stream) {
+    return fk_forward_euler_tracked(g, state, scratch, D, p, stimuli, n_stimuli, t0, t1, dt, dx,
+                                    nullptr, stream);
 }
 
 int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
@@ -310,7 +339,7 @@ int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
     Stim st[kMaxStim];
     if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
     CUtensorMap tm_d;
-    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SU_W, SD_H))) return rc;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
     if (!status) return FK_ERR_CUDA;
     const Model m = make_model(*p);

@@ -88,6 +88,19 @@ __device__ __forceinline__ bool stim_active(const Stim &s, float t) {
     return m < s.duration;
 }
 
+// 1 + tanh(x), through the identity 1 + tanh(x) = 2 / (1 + exp(-2x)), with the hardware
+// base-2 exponential and reciprocal approximations (ex2.approx, rcp.approx: a few ulp).  The
+// identity has no cancellation for x << 0 (the resting state, x ~ -8.5), where the reference
+// computes 1 + tanh(x) after rounding tanh to float32.  Saturates correctly: x -> -inf gives 0
+// (exp overflows to +inf, rcp(+inf) = 0), x -> +inf gives 2.
+__device__ __forceinline__ float one_plus_tanh(float x) {
+    const float kM2Log2e = -2.8853900817779268f;  // -2 / ln(2)
+    float e, r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x * kM2Log2e));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + e));
+    return 2.0f * r;
+}
+
 // Ionic model: gates, currents, gate derivatives (cardiax/solve.py:34-42,57-58).
 struct Reaction {
     float dv, dw, j_ion;
@@ -100,7 +113,7 @@ __device__ __forceinline__ Reaction reaction(float u, float v, float w, const Mo
     // j_so = u (1 - p) / tau_0 + p / tau_r
     float j_so = p ? m.inv_tau_r : u * m.r_tau_0;
     // j_si = -w (1 + tanh(k (u - V_csi))) / (2 tau_si)
-    float j_si = -(w * (1.0f + tanhf(m.k * (u - m.V_csi)))) * m.r_2tau_si;
+    float j_si = -(w * one_plus_tanh(m.k * (u - m.V_csi))) * m.r_2tau_si;
     Reaction r;
     r.j_ion = -((j_fi + j_so) + j_si) * m.r_Cm;
     const float r_tvm = q ? m.r_tau_v2m : m.r_tau_v1m;

@@ -42,7 +42,19 @@ __device__ __forceinline__ float uy_at(const Clamped &u, int r, int y) {
     return g_central(u.at(r, y - 2), u.at(r, y - 1), u.at(r, y + 1), u.at(r, y + 2));
 }
 
-__device__ void boundary_cell(const StepArgs &a, unsigned active, bool deriv, int i, int j) {
+// Activation bookkeeping for one cell (only touches memory on an upstroke).
+__device__ __forceinline__ void record_activation(const StepArgs &a, int64_t off, float u_old,
+                                                  float u_new) {
+    if (u_old < a.act_threshold && u_new >= a.act_threshold) {
+        const int32_t t1 = (int32_t)a.t + 1;
+        a.act_last[off] = t1;
+        if (a.act_first[off] < 0) a.act_first[off] = t1;
+        a.act_count[off] += 1;
+    }
+}
+
+template <bool ACT>
+__device__ __noinline__ void boundary_cell(const StepArgs &a, unsigned active, bool deriv, int i, int j) {
     const Clamped U{a.u, a.H, a.W, a.pitch}, D{a.D, a.H, a.W, a.pitch};
     const int H = a.H, W = a.W;
     const float rdx = a.rdx;
@@ -89,197 +101,243 @@ __device__ void boundary_cell(const StepArgs &a, unsigned active, bool deriv, in
     } else {
         a.vo[off] = fmaf(r.dv, a.dt, v);
         a.wo[off] = fmaf(r.dw, a.dt, w);
-        a.uo[off] = fmaf(du, a.dt, u);
+        const float un = fmaf(du, a.dt, u);
+        a.uo[off] = un;
+        if (ACT) record_activation(a, off, u, un);
     }
 }
 
+// Stimulus override for the 4 cells (i, j .. j+3) of one thread: later active stimuli win,
+// a zero value leaves the ionic current (cardiax/solve.py:257-271).  Out of line: it runs only
+// on the steps where some protocol is on.
+__device__ __noinline__ float4 apply_stimuli(const StepArgs &a, unsigned active, int i, int j,
+                                             int64_t goff, float4 jion4) {
+    float j_ion[4] = {jion4.x, jion4.y, jion4.z, jion4.w};
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int jj = j + m;
+        if (i >= a.H || jj >= a.W) continue;
+        float acc = 0.0f;
+        for (int s = 0; s < a.n_stim; ++s) {
+            if (!((active >> s) & 1u)) continue;
+            const Stim &st = a.stim[s];
+            const float fv = st.field ? __ldg(st.field + goff + m)
+                                      : ((i >= st.r0 && i < st.r1 && jj >= st.c0 && jj < st.c1)
+                                             ? st.amplitude : 0.0f);
+            if (fv != 0.0f) acc = fv;
+        }
+        if (acc != 0.0f) j_ion[m] = acc;
+    }
+    return make_float4(j_ion[0], j_ion[1], j_ion[2], j_ion[3]);
+}
+
+template <bool ACT>
+__device__ __noinline__ void boundary_band(const StepArgs &a, unsigned active, bool deriv, int i0,
+                                           int j0) {
+    const int ih = min(TY, a.H - i0), jw = min(TX, a.W - j0);
+    for (int idx = threadIdx.x; idx < ih * jw; idx += NT) {
+        const int i = i0 + idx / jw, jj = j0 + idx % jw;
+        if (i < BAND || i >= a.H - BAND || jj < BAND || jj >= a.W - BAND)
+            boundary_cell<ACT>(a, active, deriv, i, jj);
+    }
+}
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+
 // ---- the step kernel ----------------------------------------------------------------------
-template <bool DERIV>
-__global__ void __launch_bounds__(NT) fk_step_kernel(const __grid_constant__ CUtensorMap tm_u,
-                                                     const __grid_constant__ CUtensorMap tm_d,
-                                                     const __grid_constant__ StepArgs a) {
+template <bool DERIV, bool ACT>
+__global__ void __launch_bounds__(NT, 2) fk_step_kernel(const __grid_constant__ StepMaps tm,
+                                                        const __grid_constant__ StepArgs a) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float *su = reinterpret_cast<float *>(smem);
-    float *sd = reinterpret_cast<float *>(smem + SMEM_U_BYTES);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SMEM_U_BYTES + SMEM_D_BYTES);
+    float *su = reinterpret_cast<float *>(smem);                       // [SU_H][SW]
+    float *sd = reinterpret_cast<float *>(smem + SMEM_U_BYTES);        // [SD_H][SW]
+    float *sv = sd + SW * SD_H;                                        // [TY][TX]
+    float *sw = sv + TX * TY;                                          // [TY][TX]
+    float *sux = sw + TX * TY;                                         // [SUX_H][TX]
+    float *suy = sux + TX * SUX_H;                                     // [TY][SW]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(suy + SW * TY);
 
     const int tid = threadIdx.x;
     const int j0 = blockIdx.x * TX, i0 = blockIdx.y * TY;
     const int H = a.H, W = a.W, pitch = a.pitch;
 
     if (tid == 0) {
-        prefetch_tensormap(&tm_u);
-        prefetch_tensormap(&tm_d);
+        prefetch_tensormap(&tm.u);
+        prefetch_tensormap(&tm.v);
+        prefetch_tensormap(&tm.w);
+        prefetch_tensormap(&tm.d);
         mbar_init(bar, 1);
         fence_barrier_init();
     }
     __syncthreads();
     if (tid == 0) {
-        mbar_arrive_expect_tx(bar, SMEM_U_BYTES + SMEM_D_BYTES);
-        tma_load_2d(su, &tm_u, j0 - HALO_U, i0 - HALO_U, bar);
-        tma_load_2d(sd, &tm_d, j0 - HALO_U, i0 - HALO_D, bar);
+        mbar_arrive_expect_tx(bar, SMEM_TMA_BYTES);
+        tma_load_2d(su, &tm.u, j0 - HALO_U, i0 - HALO_U, bar);
+        tma_load_2d(sd, &tm.d, j0 - HALO_U, i0 - HALO_D, bar);
+        tma_load_2d(sv, &tm.v, j0, i0, bar);
+        tma_load_2d(sw, &tm.w, j0, i0, bar);
     }
 
-    // stimulus protocol (uniform over the launch)
+    // pass-2 ownership
+    const int tx = tid % NTX, ty = tid / NTX;
+    const int j = j0 + 4 * tx;
+    const int rbase = RPT * ty;
     unsigned active = 0;
     for (int s = 0; s < a.n_stim; ++s)
         if (stim_active(a.stim[s], a.t)) active |= 1u << s;
-
-    const int tx = tid % NTX, ty = tid / NTX;
-    const int j = j0 + 4 * tx;
-    const int r0 = MR * ty;  // first row of this thread within the tile
-    const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
-    const bool col_in = j < W;
 
     if (!mbar_wait_bounded(bar, 0)) {
         if (tid == 0) atomicOr(a.status, kStatusTimeout);
         return;
     }
-
     const float rdx = a.rdx;
-    const float *su_c = su + 4 * tx + HALO_U;  // this thread's first column, u tile
-    const float *sd_c = sd + 4 * tx + HALO_U;  // this thread's first column, D tile
-    auto LU = [&](int row) { return *reinterpret_cast<const float4 *>(su_c + row * SU_W); };
-    auto LUo = [&](int row, int dcol) {
-        return *reinterpret_cast<const float4 *>(su_c + row * SU_W + dcol);
-    };
-    auto LD = [&](int row) { return *reinterpret_cast<const float4 *>(sd_c + row * SU_W); };
-    auto LDo = [&](int row, int dcol) {
-        return *reinterpret_cast<const float4 *>(sd_c + row * SU_W + dcol);
-    };
 
-    // u rows of the vertical window, in u-tile rows (tile row + HALO_U)
-    const int ub = r0 + HALO_U;
-    float4 w0 = LU(ub - 4), w1 = LU(ub - 3), w2 = LU(ub - 2), w3 = LU(ub - 1), w4 = LU(ub);
-    float4 x0 = mul4(g_central4(w0, w1, w3, w4), rdx);  // u_x at tile row r0-2
-    w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = LU(ub + 1);
-    float4 x1 = mul4(g_central4(w0, w1, w3, w4), rdx);  // r0-1
-    w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = LU(ub + 2);
-    float4 x2 = mul4(g_central4(w0, w1, w3, w4), rdx);  // r0
-    w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = LU(ub + 3);
-    float4 x3 = mul4(g_central4(w0, w1, w3, w4), rdx);  // r0+1
-    // D rows of the vertical window, in D-tile rows (tile row + HALO_D)
-    const int db = r0 + HALO_D;
-    float4 d0 = LD(db - 2), d1 = LD(db - 1), d2 = LD(db), d3 = LD(db + 1), d4;
+    // ---- pass 1: u_x (tile rows -2 .. TY+1) and u_y (tile columns -2 .. TX+1) -------------
+#pragma unroll 1
+    for (int it = tid; it < SUX_H * NTX; it += NT) {
+        const int r = it / NTX, q = it % NTX;
+        const float *b = su + (r + 2) * SW + HALO_U + 4 * q;
+        st4(sux + r * TX + 4 * q,
+            mul4(g_central4(ld4(b - 2 * SW), ld4(b - SW), ld4(b + SW), ld4(b + 2 * SW)), rdx));
+    }
+#pragma unroll 1
+    for (int it = tid; it < TY * NTX; it += NT) {
+        const int r = it / NTX, q = it % NTX;
+        const float *b = su + (r + HALO_U) * SW + 4 * q;  // columns j0+4q-4 .. j0+4q+7
+        const float4 x0 = ld4(b), x1 = ld4(b + 4), x2 = ld4(b + 8);
+        const float e[12] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
+                             x2.x, x2.y, x2.z, x2.w};
+        float4 o;
+        o.x = g_central(e[2], e[3], e[5], e[6]) * rdx;
+        o.y = g_central(e[3], e[4], e[6], e[7]) * rdx;
+        o.z = g_central(e[4], e[5], e[7], e[8]) * rdx;
+        o.w = g_central(e[5], e[6], e[8], e[9]) * rdx;
+        st4(suy + r * SW + HALO_U + 4 * q, o);
+    }
+    if (tid < TY * 4) {  // the 2 + 2 halo columns of u_y
+        const int r = tid / 4, k = tid % 4;
+        const int c = k < 2 ? 2 + k : TX + HALO_U + (k - 2);  // same column index in su and suy
+        const float *row = su + (r + HALO_U) * SW;
+        suy[r * SW + c] = g_central(row[c - 2], row[c - 1], row[c + 1], row[c + 2]) * rdx;
+    }
+    __syncthreads();
 
-#pragma unroll
-    for (int rr = 0; rr < MR; ++rr) {
-        const int i = i0 + r0 + rr;
+    // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
+    const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
+#pragma unroll 1
+    for (int k = 0; k < RPT; ++k) {
+        const int r = rbase + k;
+        const int i = i0 + r;
         const int64_t goff = (int64_t)i * pitch + j;
-        float4 v4 = make_float4(0.f, 0.f, 0.f, 0.f), wv4 = v4;
-        if (i < H && col_in) {
-            v4 = __ldg(reinterpret_cast<const float4 *>(a.v + goff));
-            wv4 = __ldg(reinterpret_cast<const float4 *>(a.w + goff));
-        }
-        // vertical u: window now centred two rows below this cell
-        w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = LU(ub + rr + 4);
-        const float4 x4 = mul4(g_central4(w0, w1, w3, w4), rdx);  // u_x at r0+rr+2
-        const float4 uxx = mul4(g_central4(x0, x1, x3, x4), rdx);
-        const float4 uxc = x2;
-        const float4 uc = w0;  // u at this cell row
-        // horizontal u: columns j-4 .. j+7
-        const float4 ul = LUo(ub + rr, -4), ur = LUo(ub + rr, 4);
-        const float e[12] = {ul.x, ul.y, ul.z, ul.w, uc.x, uc.y, uc.z, uc.w,
-                             ur.x, ur.y, ur.z, ur.w};
-        float uy[8];  // u_y at columns j-2 .. j+5
-#pragma unroll
-        for (int m = 0; m < 8; ++m) uy[m] = g_central(e[m], e[m + 1], e[m + 3], e[m + 4]) * rdx;
-        float uyy[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) uyy[m] = g_central(uy[m], uy[m + 1], uy[m + 3], uy[m + 4]) * rdx;
-        // D and its derivatives
-        d4 = LD(db + rr + 2);
-        const float4 dxD = mul4(g_central4(d0, d1, d3, d4), rdx);
-        const float4 dc = d2;
-        const float4 dl = LDo(db + rr, -4), dr = LDo(db + rr, 4);
-        const float f[12] = {dl.x, dl.y, dl.z, dl.w, dc.x, dc.y, dc.z, dc.w,
+        const float *xb = sux + (r + 2) * TX + 4 * tx;
+        const float4 uxc = ld4(xb);
+        const float4 uxx = mul4(g_central4(ld4(xb - 2 * TX), ld4(xb - TX), ld4(xb + TX),
+                                           ld4(xb + 2 * TX)), rdx);
+        const float *yb = suy + r * SW + 4 * tx;
+        const float4 y0 = ld4(yb), y1 = ld4(yb + 4), y2 = ld4(yb + 8);
+        const float f[12] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w,
+                             y2.x, y2.y, y2.z, y2.w};
+        const float *db = sd + (r + HALO_D) * SW + HALO_U + 4 * tx;
+        const float4 dc = ld4(db);
+        const float4 dxD = mul4(g_central4(ld4(db - 2 * SW), ld4(db - SW), ld4(db + SW),
+                                           ld4(db + 2 * SW)), rdx);
+        const float4 dl = ld4(db - 4), dr = ld4(db + 4);
+        const float g[12] = {dl.x, dl.y, dl.z, dl.w, dc.x, dc.y, dc.z, dc.w,
                              dr.x, dr.y, dr.z, dr.w};
-        float dyD[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) dyD[m] = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]) * rdx;
+        const float4 uc = ld4(su + (r + HALO_U) * SW + HALO_U + 4 * tx);
+        const float4 vc = ld4(sv + r * TX + 4 * tx), wc = ld4(sw + r * TX + 4 * tx);
 
         const float uu[4] = {uc.x, uc.y, uc.z, uc.w};
-        const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
-        const float ww[4] = {wv4.x, wv4.y, wv4.z, wv4.w};
+        const float vv[4] = {vc.x, vc.y, vc.z, vc.w};
+        const float ww[4] = {wc.x, wc.y, wc.z, wc.w};
         const float dd[4] = {dc.x, dc.y, dc.z, dc.w};
         const float dxv[4] = {dxD.x, dxD.y, dxD.z, dxD.w};
         const float uxv[4] = {uxc.x, uxc.y, uxc.z, uxc.w};
         const float uxxv[4] = {uxx.x, uxx.y, uxx.z, uxx.w};
-        float ov[4], ow[4], ou[4];
+        float ov[4], ow[4], ou[4], jion[4], dv[4], dw[4];
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            Reaction r = reaction(uu[m], vv[m], ww[m], a.m);
-            if (active) {
-                float acc = 0.0f;
-                for (int s = 0; s < a.n_stim; ++s) {
-                    if (!((active >> s) & 1u)) continue;
-                    const Stim &st = a.stim[s];
-                    const int jj = j + m;
-                    float fv;
-                    if (st.field) fv = (i < H && jj < W) ? __ldg(st.field + goff + m) : 0.0f;
-                    else fv = (i >= st.r0 && i < st.r1 && jj >= st.c0 && jj < st.c1) ? st.amplitude : 0.0f;
-                    if (fv != 0.0f) acc = fv;
-                }
-                if (acc != 0.0f) r.j_ion = acc;
-            }
-            const float du = diffusion(dd[m], dxv[m], dyD[m], uxv[m], uy[m + 2], uxxv[m], uyy[m]) + r.j_ion;
+            const Reaction re = reaction(uu[m], vv[m], ww[m], a.m);
+            jion[m] = re.j_ion;
+            dv[m] = re.dv;
+            dw[m] = re.dw;
+        }
+        if (active) {
+            const float4 js = apply_stimuli(a, active, i, j, goff,
+                                            make_float4(jion[0], jion[1], jion[2], jion[3]));
+            jion[0] = js.x;
+            jion[1] = js.y;
+            jion[2] = js.z;
+            jion[3] = js.w;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const float uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]) * rdx;
+            const float dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]) * rdx;
+            const float du = diffusion(dd[m], dxv[m], dyD, uxv[m], f[m + 4], uxxv[m], uyy) + jion[m];
             if (DERIV) {
-                ov[m] = r.dv;
-                ow[m] = r.dw;
+                ov[m] = dv[m];
+                ow[m] = dw[m];
                 ou[m] = du;
             } else {
-                ov[m] = fmaf(r.dv, a.dt, vv[m]);
-                ow[m] = fmaf(r.dw, a.dt, ww[m]);
+                ov[m] = fmaf(dv[m], a.dt, vv[m]);
+                ow[m] = fmaf(dw[m], a.dt, ww[m]);
                 ou[m] = fmaf(du, a.dt, uu[m]);
             }
         }
-        // store: whole float4 inside the band-free interior, else only the interior cells
         if (interior) {
-            *reinterpret_cast<float4 *>(a.vo + goff) = make_float4(ov[0], ov[1], ov[2], ov[3]);
-            *reinterpret_cast<float4 *>(a.wo + goff) = make_float4(ow[0], ow[1], ow[2], ow[3]);
-            *reinterpret_cast<float4 *>(a.uo + goff) = make_float4(ou[0], ou[1], ou[2], ou[3]);
-        } else if (i >= BAND && i < H - BAND) {
-            const bool full = j >= BAND && j + 3 < W - BAND;
-            if (full) {
-                *reinterpret_cast<float4 *>(a.vo + goff) = make_float4(ov[0], ov[1], ov[2], ov[3]);
-                *reinterpret_cast<float4 *>(a.wo + goff) = make_float4(ow[0], ow[1], ow[2], ow[3]);
-                *reinterpret_cast<float4 *>(a.uo + goff) = make_float4(ou[0], ou[1], ou[2], ou[3]);
-            } else {
+            st4(a.vo + goff, make_float4(ov[0], ov[1], ov[2], ov[3]));
+            st4(a.wo + goff, make_float4(ow[0], ow[1], ow[2], ow[3]));
+            st4(a.uo + goff, make_float4(ou[0], ou[1], ou[2], ou[3]));
+            if (ACT && !DERIV) {
 #pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    const int jj = j + m;
-                    if (jj >= BAND && jj < W - BAND) {
-                        a.vo[goff + m] = ov[m];
-                        a.wo[goff + m] = ow[m];
-                        a.uo[goff + m] = ou[m];
-                    }
+                for (int m = 0; m < 4; ++m) record_activation(a, goff + m, uu[m], ou[m]);
+            }
+        } else if (i >= BAND && i < H - BAND) {
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                const int jj = j + m;
+                if (jj >= BAND && jj < W - BAND) {
+                    a.vo[goff + m] = ov[m];
+                    a.wo[goff + m] = ow[m];
+                    a.uo[goff + m] = ou[m];
+                    if (ACT && !DERIV) record_activation(a, goff + m, uu[m], ou[m]);
                 }
             }
         }
-        x0 = x1; x1 = x2; x2 = x3; x3 = x4;
-        d0 = d1; d1 = d2; d2 = d3; d3 = d4;
     }
 
-    if (!interior) {
-        // cells of this tile within BAND of an edge
-        const int ih = min(TY, H - i0), jw = min(TX, W - j0);
-        for (int idx = tid; idx < ih * jw; idx += NT) {
-            const int i = i0 + idx / jw, jj = j0 + idx % jw;
-            if (i < BAND || i >= H - BAND || jj < BAND || jj >= W - BAND)
-                boundary_cell(a, active, DERIV, i, jj);
-        }
-    }
+    if (!interior) boundary_band<ACT && !DERIV>(a, active, DERIV, i0, j0);
 }
 
-cudaError_t launch_step(const CUtensorMap &tm_u, const CUtensorMap &tm_d, const StepArgs &a,
-                        bool deriv, cudaStream_t stream) {
+template <bool DERIV, bool ACT>
+static cudaError_t set_smem_attr() {
+    return cudaFuncSetAttribute(fk_step_kernel<DERIV, ACT>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_STEP_BYTES);
+}
+
+cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream) {
+    // the attribute is per function and per device; setting it is cheap and idempotent
+    static thread_local int configured_device = -1;
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != configured_device) {
+        cudaError_t e;
+        if ((e = set_smem_attr<true, false>()) != cudaSuccess) return e;
+        if ((e = set_smem_attr<false, true>()) != cudaSuccess) return e;
+        if ((e = set_smem_attr<false, false>()) != cudaSuccess) return e;
+        configured_device = dev;
+    }
     dim3 grid((a.W + TX - 1) / TX, (a.H + TY - 1) / TY);
     if (deriv)
-        fk_step_kernel<true><<<grid, NT, SMEM_STEP_BYTES, stream>>>(tm_u, tm_d, a);
+        fk_step_kernel<true, false><<<grid, NT, SMEM_STEP_BYTES, stream>>>(maps, a);
+    else if (a.act_last)
+        fk_step_kernel<false, true><<<grid, NT, SMEM_STEP_BYTES, stream>>>(maps, a);
     else
-        fk_step_kernel<false><<<grid, NT, SMEM_STEP_BYTES, stream>>>(tm_u, tm_d, a);
+        fk_step_kernel<false, false><<<grid, NT, SMEM_STEP_BYTES, stream>>>(maps, a);
     return cudaGetLastError();
 }
 

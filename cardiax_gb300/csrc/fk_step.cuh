@@ -8,22 +8,28 @@
 
 namespace fk {
 
-// Tile geometry of the single-step kernel: a CTA owns TY x TX cells; each thread owns a
-// 4-column x MR-row micro-tile (float4 columns, MR rows streamed top to bottom).
+// Tile geometry of the step kernel.  A CTA of NT threads owns TY x TX cells.
+//   pass 1: u_x on rows -2 .. TY+1 and u_y on columns -2 .. TX+1 go to shared memory;
+//   pass 2: thread (tx, ty) owns columns 4tx .. 4tx+3 of rows RPT*ty .. RPT*ty+RPT-1.
 constexpr int TX = 128;
 constexpr int TY = 32;
-constexpr int MR = 8;
-constexpr int NTX = TX / 4;
-constexpr int NTY = TY / MR;
-constexpr int NT = NTX * NTY;
+constexpr int NT = 256;
+constexpr int NTX = TX / 4;          // float4 columns
+constexpr int RPT = TY / (NT / NTX); // rows per thread in pass 2
 constexpr int HALO_U = 4;  // u_xx composes two radius-2 derivatives
 constexpr int HALO_D = 2;  // D_x is one radius-2 derivative
-constexpr int SU_W = TX + 2 * HALO_U;   // u box width (also used for D: 16-byte alignment)
+constexpr int SW = TX + 2 * HALO_U;   // row width of the u, D and u_y tiles (16-byte multiple)
 constexpr int SU_H = TY + 2 * HALO_U;
 constexpr int SD_H = TY + 2 * HALO_D;
-constexpr int SMEM_U_BYTES = SU_W * SU_H * 4;
-constexpr int SMEM_D_BYTES = SU_W * SD_H * 4;
-constexpr int SMEM_STEP_BYTES = SMEM_U_BYTES + SMEM_D_BYTES + 16 + 128;  // + mbarrier + align
+constexpr int SUX_H = TY + 4;         // u_x rows -2 .. TY+1
+constexpr int SMEM_U_BYTES = SW * SU_H * 4;
+constexpr int SMEM_D_BYTES = SW * SD_H * 4;
+constexpr int SMEM_UX_BYTES = TX * SUX_H * 4;
+constexpr int SMEM_UY_BYTES = SW * TY * 4;
+constexpr int SMEM_VW_BYTES = TX * TY * 4;  // one of the v, w tiles (no halo)
+constexpr int SMEM_TMA_BYTES = SMEM_U_BYTES + SMEM_D_BYTES + 2 * SMEM_VW_BYTES;
+constexpr int SMEM_STEP_BYTES =
+    SMEM_TMA_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES + 16 + 128;  // + mbarrier + align
 // Cells within this distance of an edge take the per-cell boundary path (one-sided stencils
 // and edge padding reach 4 cells in).
 constexpr int BAND = 4;
@@ -39,12 +45,23 @@ struct StepArgs {
     Model m;
     Stim stim[kMaxStim];
     int *status;  // device error word: set on a barrier timeout
+    // activation tracking (upstrokes of u through `act_threshold`); null when off
+    int32_t *act_first, *act_last, *act_count;
+    float act_threshold;
 };
 
 enum : int { kStatusTimeout = 1 };
 
-// Launches one step (Euler update, or the derivative when `deriv`).
-cudaError_t launch_step(const CUtensorMap &tm_u, const CUtensorMap &tm_d, const StepArgs &a,
-                        bool deriv, cudaStream_t stream);
+// TMA descriptors of one step: u (box SW x SU_H), v and w (box TX x TY) of the input state,
+// and D (box SW x SD_H).
+struct StepMaps {
+    CUtensorMap u, v, w, d;
+};
+
+// Launches one step (Euler update, or the derivative when `deriv`).  With a.act_last set, the
+// Euler step also records activations: a cell whose u goes from below the threshold to at or
+// above it during step t -> t+1 gets act_last = t+1, act_first = t+1 if it was -1, and
+// act_count + 1.
+cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream);
 
 }  // namespace fk

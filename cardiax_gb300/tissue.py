@@ -134,6 +134,7 @@ class Tissue:
                                                                 self.device)
             self.state = torch.empty((3, H, self.pitch), dtype=torch.float32, device=self.device)
             self.scratch = torch.empty_like(self.state)
+        self.activation = None
         self.init()
 
     # -- state ----------------------------------------------------------------------------
@@ -153,12 +154,30 @@ class Tissue:
         buf = self.state if buf is None else buf
         return buf[..., 0, :, :self.W], buf[..., 1, :, :self.W], buf[..., 2, :, :self.W]
 
+    def track_activation(self, threshold: float = 0.5) -> "Tissue":
+        """Records activation times during ``advance``: an upstroke of u through ``threshold``
+        during step t -> t+1 is recorded as t+1 in ``act_first`` (first one), ``act_last`` (most
+        recent) and counted in ``act_count`` (int32 (H, pitch) planes; -1 / 0 when none)."""
+        kw = dict(dtype=torch.int32, device=self.device)
+        self.act_first = torch.full((self.H, self.pitch), -1, **kw)
+        self.act_last = torch.full((self.H, self.pitch), -1, **kw)
+        self.act_count = torch.zeros((self.H, self.pitch), **kw)
+        self.activation = N.Activation(self.act_first.data_ptr(), self.act_last.data_ptr(),
+                                       self.act_count.data_ptr(), float(threshold))
+        return self
+
+    def activation_maps(self):
+        """(first, last, count) activation maps without the padding columns."""
+        W = self.W
+        return self.act_first[:, :W], self.act_last[:, :W], self.act_count[:, :W]
+
     # -- stepping -------------------------------------------------------------------------
     def advance(self, t0: int, t1: int) -> "Tissue":
         """Steps t0 .. t1-1 in place (cardiax/solve.py:92-100)."""
-        N.call("fk_forward_euler", self.grid, self.state.data_ptr(), self.scratch.data_ptr(),
-               self.D.data_ptr(), ctypes.byref(self.params), self.stim, self.n_stim,
-               int(t0), int(t1), self.dt, self.dx, stream_handle())
+        act = ctypes.byref(self.activation) if self.activation is not None else None
+        N.call("fk_forward_euler_tracked", self.grid, self.state.data_ptr(),
+               self.scratch.data_ptr(), self.D.data_ptr(), ctypes.byref(self.params), self.stim,
+               self.n_stim, int(t0), int(t1), self.dt, self.dx, act, stream_handle())
         return self
 
     def forward(self, checkpoints, out: torch.Tensor = None) -> torch.Tensor:

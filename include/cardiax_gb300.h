@@ -101,6 +101,22 @@ int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
                const int64_t *checkpoints, int n_checkpoints, double dt, double dx, float *out,
                void *stream);
 
+/* Activation-time maps (int32 planes with the grid's pitch).  An activation is an upstroke of u
+ * through `threshold` during step t -> t+1; it is recorded as time t+1: `last` = t+1, `first` =
+ * t+1 if it was negative, `count` += 1.  Initialise first/last to -1 and count to 0.  The
+ * reference has no activation metric (its cardiax/metrics.py stubs are empty); these maps are
+ * what long chaotic runs are compared on. */
+typedef struct {
+    int32_t *first, *last, *count;
+    float threshold;
+} fk_activation;
+
+/* fk_forward_euler with activation tracking (`act` may be NULL: plain stepping). */
+int fk_forward_euler_tracked(fk_grid g, float *state, float *scratch, const float *D,
+                             const fk_params *p, const fk_stimulus *stimuli, int n_stimuli,
+                             int64_t t0, int64_t t1, double dt, double dx,
+                             const fk_activation *act, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -133,7 +133,9 @@ typedef struct {
     }                                                                                          \
     int fko_forward_euler_##SUF(T *v, T *w, T *u, const T *D, long H, long W,                  \
                                 const double *params, const fko_stim *stims, int n_stims,      \
-                                long t0, long t1, double dt, double dx, int nthreads) {        \
+                                long t0, long t1, double dt, double dx, int nthreads,          \
+                                int *act_first, int *act_last, int *act_count,                 \
+                                double threshold) {                                            \
         if (H < 3 || W < 3) return -2;                                                         \
         if (nthreads < 1) nthreads = 1;                                                        \
         ws_##SUF ws;                                                                           \
@@ -159,6 +161,16 @@ typedef struct {
             rc = step_##SUF(&ws, v, w, u, bv, bw, bu, D, params, stims, n_stims, (T)s, k, h,   \
                             nthreads);                                                         \
             if (rc) goto done;                                                                 \
+            if (act_last) {                                                                    \
+                /* activation: upstroke of u through the threshold during step s -> s+1 */     \
+                const T thr = (T)threshold;                                                    \
+                for (size_t c = 0; c < n; ++c)                                                 \
+                    if (u[c] < thr && bu[c] >= thr) {                                          \
+                        act_last[c] = (int)(s + 1);                                            \
+                        if (act_first[c] < 0) act_first[c] = (int)(s + 1);                     \
+                        act_count[c] += 1;                                                     \
+                    }                                                                          \
+            }                                                                                  \
             memcpy(v, bv, sizeof(T) * n); memcpy(w, bw, sizeof(T) * n);                        \
             memcpy(u, bu, sizeof(T) * n);                                                      \
         }                                                                                      \

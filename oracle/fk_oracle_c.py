@@ -43,7 +43,9 @@ def _load():
                                                    ctypes.POINTER(ctypes.c_double),
                                                    ctypes.POINTER(_Stim), ctypes.c_int,
                                                    ctypes.c_long, ctypes.c_long,
-                                                   ctypes.c_double, ctypes.c_double, ctypes.c_int]
+                                                   ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                   ctypes.c_void_p, ctypes.c_void_p,
+                                                   ctypes.c_void_p, ctypes.c_double]
         lib.fko_max_threads.restype = ctypes.c_int
         _lib = lib
     return _lib
@@ -53,11 +55,14 @@ def max_threads() -> int:
     return int(_load().fko_max_threads())
 
 
-def forward_euler(state, t0, t1, params, diffusivity, stimuli, dt, dx, threads: int = 1):
+def forward_euler(state, t0, t1, params, diffusivity, stimuli, dt, dx, threads: int = 1,
+                  activation=None):
     """Advance ``state`` = (v, w, u) from step t0 to t1; returns new arrays (v, w, u).
 
     ``stimuli``: sequence of (start, duration, period, field) in steps.  The working type is the
-    dtype of ``state`` (float32 or float64).
+    dtype of ``state`` (float32 or float64).  ``activation``: optional (first, last, count,
+    threshold) with int32 (H, W) arrays updated in place -- an upstroke of u through the threshold
+    during step s -> s+1 records time s+1.
     """
     lib = _load()
     dtype = np.dtype(state[0].dtype)
@@ -70,8 +75,15 @@ def forward_euler(state, t0, t1, params, diffusivity, stimuli, dt, dx, threads: 
     arr = (_Stim * max(1, len(stimuli)))()
     for i, s in enumerate(stimuli):
         arr[i] = _Stim(float(s[0]), float(s[1]), float(s[2]), fields[i].ctypes.data)
+    if activation is not None:
+        first, last, count, thr = activation
+        for a in (first, last, count):
+            assert a.dtype == np.int32 and a.flags.c_contiguous and a.shape == (H, W)
+        act = (first.ctypes.data, last.ctypes.data, count.ctypes.data, float(thr))
+    else:
+        act = (None, None, None, 0.0)
     rc = fn(v.ctypes.data, w.ctypes.data, u.ctypes.data, D.ctypes.data, H, W, prm, arr,
-            len(stimuli), int(t0), int(t1), float(dt), float(dx), int(threads))
+            len(stimuli), int(t0), int(t1), float(dt), float(dx), int(threads), *act)
     if rc != 0:
         raise RuntimeError(f"C oracle failed with status {rc}")
     return v, w, u

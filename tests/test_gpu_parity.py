@@ -199,16 +199,21 @@ def _c_oracle():
     return C
 
 
+def _roofline_D(H, W, seed):
+    import bench
+    return bench.noisy_diffusivity(H, W, seed)
+
+
 def test_full_size_2048_subthreshold_arithmetic():
-    """2048x2048 with the roofline D map (5% per-cell noise) and a smooth sub-threshold state
-    (u < V_v everywhere, so no gate can flip): 100 steps vs the C oracle.  This isolates the
-    stencil and diffusion arithmetic at full size; the bound reflects last-bit differences."""
+    """2048x2048 with the roofline D map (5% noise) and a smooth sub-threshold state (u < V_v
+    everywhere, so no gate can flip): 100 steps vs the C oracle.  This isolates the stencil and
+    diffusion arithmetic at full size; the bound reflects last-bit differences."""
     _gpu()
     C = _c_oracle()
     from cardiax_gb300 import solve
     H = W = 2048
     rng = np.random.default_rng(3)
-    D = np.clip(0.001 * (1 + 0.05 * rng.standard_normal((H, W))), 0, None).astype(np.float32)
+    D = _roofline_D(H, W, 3)
     st0 = O.init((H, W))
     st0.u[:, :] = _smooth(rng, (H, W), 0.0, 0.03)
     ref = C.forward_euler(st0, 0, 100, P3, D, [], 0.01, 0.01, threads=C.max_threads())
@@ -228,8 +233,7 @@ def test_full_size_2048_planar_wave():
     from cardiax_gb300 import solve
     from cardiax_gb300.stimulus import Protocol, Stimulus
     H = W = 2048
-    rng = np.random.default_rng(5)
-    D = np.clip(0.001 * (1 + 0.05 * rng.standard_normal((H, W))), 0, None).astype(np.float32)
+    D = _roofline_D(H, W, 5)
     f = np.zeros((H, W), np.float32)
     f[:, :5] = 20.0
     ref = C.forward_euler(O.init((H, W)), 0, 400, P3, D, [(0, 200, 20000, f)], 0.01, 0.01,
@@ -237,8 +241,35 @@ def test_full_size_2048_planar_wave():
     got = solve._forward_euler(solve.init((H, W)), 0, 400, P3, D,
                                [Stimulus(Protocol(0, 200, 20000), f)], 0.01, 0.01)
     gu = _np(got.u)
-    assert float(gu[:, 20].min()) > 0.5  # the wave has travelled past column 20
+    assert float(gu[:, 12].min()) > 0.5  # the wave has travelled past column 12
     assert np.abs(gu - ref[2]).max() <= TOL_U_1000
     for a, b in zip(got[:2], ref[:2]):
         d = np.abs(_np(a) - b)
         assert (d > 1e-4).mean() <= 1e-5 and d.max() <= 1e-2
+
+
+def test_activation_times_within_one_step():
+    """Activation-time maps (first upstroke through u = 0.5) of a planar wave plus a later
+    point stimulus on 256x256 with a scar-like D, 3000 steps: GPU vs the C oracle, every cell
+    within one step."""
+    _gpu()
+    C = _c_oracle()
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    from cardiax_gb300.tissue import Tissue
+    H = W = 256
+    rng = np.random.default_rng(11)
+    D = _smooth(rng, (H, W), 1e-4, 1e-3)
+    f1 = np.zeros((H, W), np.float32); f1[:, :5] = 20.0
+    f2 = np.zeros((H, W), np.float32); f2[200:210, 100:110] = 20.0
+    stims = [(0, 2, 1e9, f1), (1500, 2, 1e9, f2)]
+    first = np.full((H, W), -1, np.int32); last = first.copy(); count = np.zeros((H, W), np.int32)
+    C.forward_euler(O.init((H, W)), 0, 3000, P3, D, stims, 0.01, 0.01,
+                    threads=C.max_threads(), activation=(first, last, count, 0.5))
+    tis = Tissue((H, W), P3, D, [Stimulus(Protocol(*s[:3]), s[3]) for s in stims])
+    tis.track_activation(0.5).advance(0, 3000)
+    gf, gl, gc = (_np(x) for x in tis.activation_maps())
+    assert (first >= 0).mean() > 0.9  # the wave reached most of the tissue
+    assert np.array_equal(gf >= 0, first >= 0)
+    assert np.abs(gf - first).max() <= 1
+    assert np.abs(gl - last).max() <= 1
+    assert np.array_equal(gc, count)
