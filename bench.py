@@ -54,6 +54,98 @@ def noisy_diffusivity(H: int, W: int, seed: int, sigma_cells: float = 2.0):
     return np.clip(0.001 * (1.0 + 0.05 * n), 0.0, None).astype(np.float32)
 
 
+def scar_diffusivity(rng, H: int, W: int, blur: float = 2.0):
+    """D = 0.001 with 1-4 elliptical scars (semi-axes 20-80 cells, random orientation) scaled by
+    a factor in [0, 0.1], floored at 1e-4 (the reference's own D domain, deepx/generate.py:80;
+    below it the reference's scheme is unstable inside scars) and blurred over ``blur`` cells."""
+    from scipy.ndimage import gaussian_filter
+
+    i, j = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    D = np.full((H, W), 1e-3)
+    for _ in range(int(rng.integers(1, 5))):
+        a, b = rng.uniform(20, 80, 2)
+        th = rng.uniform(0, np.pi)
+        ci, cj = rng.uniform(0, H), rng.uniform(0, W)
+        x = (i - ci) * np.cos(th) + (j - cj) * np.sin(th)
+        y = -(i - ci) * np.sin(th) + (j - cj) * np.cos(th)
+        D[(x / a) ** 2 + (y / b) ** 2 <= 1] *= rng.uniform(0.0, 0.1)
+    D = np.maximum(D, 1e-4)
+    return gaussian_filter(D, blur, mode="reflect").astype(np.float32)
+
+
+BATCH_SHAPES = ((64, 64), (128, 128), (256, 256), (512, 512), (256, 1024))
+
+
+def batched_workload(n: int = 256, seed: int = 99):
+    """The mixed batch: sizes from BATCH_SHAPES, parameter sets {1A, 3, 4A, 5}, scar D maps, a
+    planar (left 5 columns) or 10x10 point stimulus of amplitude 20 at a random site, start in
+    [0, 5000] steps, period in [15000, 40000] steps, duration 200 steps."""
+    from cardiax_gb300 import params as Pm
+
+    sets = (Pm.PARAMSET_1A, Pm.PARAMSET_3, Pm.PARAMSET_4A, Pm.PARAMSET_5)
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        H, W = BATCH_SHAPES[int(rng.integers(0, len(BATCH_SHAPES)))]
+        P = sets[int(rng.integers(0, 4))]
+        D = scar_diffusivity(rng, H, W)
+        f = np.zeros((H, W), np.float32)
+        if rng.uniform() < 0.5:
+            f[:, :5] = 20.0
+        else:
+            r, c = int(rng.integers(0, H - 10)), int(rng.integers(0, W - 10))
+            f[r:r + 10, c:c + 10] = 20.0
+        proto = (int(rng.integers(0, 5001)), 200, int(rng.integers(15000, 40001)))
+        out.append(((H, W), P, D, f, proto))
+    return out
+
+
+def run_batched(steps: int, reps: int, dev):
+    """GCUPS of the batched path (autotuned graph replay) and of a loop of single-tissue calls
+    over the same tissues, on the same GPU."""
+    import torch
+    from cardiax_gb300.autotune import tune_batch
+    from cardiax_gb300.batch import TissueBatch
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    from cardiax_gb300.tissue import Tissue
+
+    spec = batched_workload()
+    tissues = [Tissue(shape, P, D, [Stimulus(Protocol(*proto), f)], device=dev)
+               for shape, P, D, f, proto in spec]
+    cells = sum(t.H * t.W for t in tissues)
+    batch = TissueBatch(tissues)
+    tune = tune_batch(batch, trial_steps=128)
+
+    def timed(fn):
+        for t in tissues:
+            t.init()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    timed(lambda: batch.advance(0, steps))  # warm-up
+    tb = min(timed(lambda: batch.advance(0, steps)) for _ in range(reps))
+
+    def loop():
+        for t in tissues:
+            t.advance(0, steps)
+
+    timed(loop)
+    tl = min(timed(loop) for _ in range(reps))
+    batch.close()
+    return {"tissues": len(tissues), "cells": cells, "euler_steps": steps,
+            "gcups": cells * steps / tb / 1e9, "plain_loop_gcups": cells * steps / tl / 1e9,
+            "speedup_vs_plain_loop": tl / tb, "graph_steps": tune["graph_steps"],
+            "autotune_ms_per_step": {str(k): v for k, v in tune["ms_per_step"].items()},
+            "workload": "256 tissues, sizes {64^2,128^2,256^2,512^2,256x1024}, sets "
+                        "{1A,3,4A,5}, scar D (factor U[0,0.1], floor 1e-4, blur 2), plane or "
+                        "10x10 point stimulus, start U[0,5000], period U[15000,40000] steps"}
+
+
 def workload(H: int, W: int, seed: int = 1234):
     D = noisy_diffusivity(H, W, seed)
     field = np.zeros((H, W), np.float32)
@@ -303,6 +395,10 @@ def run_ours(args):
                 "algorithmic_bytes_per_launch": BYTES_PER_UPDATE * H * W,
                 "avg_launch_us": launch_ms * 1e3}
 
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(args.batched_steps, 2, dev)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -317,7 +413,7 @@ def run_ours(args):
                "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
                "config": config(args), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-               "gpu_launches": args.steps * (S + 1), "clocks": clk,
+               "gpu_launches": args.steps * (S + 1), "clocks": clk, "batched": batched,
                "wall_s_timed_region": t_wall}
         print(json.dumps(out))
     if world > 1:
@@ -337,6 +433,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-steps", type=int, default=2000)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -45,6 +45,13 @@ class Activation(ctypes.Structure):
                 ("threshold", ctypes.c_float)]
 
 
+class TissueDesc(ctypes.Structure):
+    _fields_ = [("g", Grid), ("state", ctypes.c_void_p), ("scratch", ctypes.c_void_p),
+                ("D", ctypes.c_void_p), ("params", Params),
+                ("stimuli", ctypes.POINTER(Stimulus)), ("n_stimuli", ctypes.c_int),
+                ("dt", ctypes.c_double), ("dx", ctypes.c_double), ("act", Activation)]
+
+
 _lib = None
 _lock = threading.Lock()
 _P = ctypes.c_void_p
@@ -67,6 +74,11 @@ _SIGNATURES = {
     "fk_forward_euler_tracked": [Grid, _P, _P, _P, ctypes.POINTER(Params),
                                  ctypes.POINTER(Stimulus), _INT, _I64, _I64, _D, _D,
                                  ctypes.POINTER(Activation), _P],
+    "fk_batch_create": [ctypes.POINTER(TissueDesc), _INT, _P, ctypes.c_size_t, _P,
+                        ctypes.POINTER(_P)],
+    "fk_batch_forward_euler": [_P, _I64, _I64, _INT, _P],
+    "fk_batch_set_grid": [_P, _INT],
+    "fk_batch_destroy": [_P],
 }
 
 
@@ -89,6 +101,8 @@ def lib(build: bool = True):
                 fn = getattr(L, name)
                 fn.restype = _INT
                 fn.argtypes = args
+            L.fk_batch_workspace_bytes.restype = ctypes.c_size_t
+            L.fk_batch_workspace_bytes.argtypes = [ctypes.POINTER(TissueDesc), _INT]
             _lib = L
     return _lib
 
@@ -100,4 +114,4 @@ def call(name: str, *args) -> None:
 
 
 def exported_symbols():
-    return ["fk_status_string"] + list(_SIGNATURES)
+    return ["fk_status_string", "fk_batch_workspace_bytes"] + list(_SIGNATURES)

@@ -43,10 +43,10 @@ __device__ __forceinline__ float uy_at(const Clamped &u, int r, int y) {
 }
 
 // Activation bookkeeping for one cell (only touches memory on an upstroke).
-__device__ __forceinline__ void record_activation(const StepArgs &a, int64_t off, float u_old,
-                                                  float u_new) {
+__device__ __forceinline__ void record_activation(const StepArgs &a, float t, int64_t off,
+                                                  float u_old, float u_new) {
     if (u_old < a.act_threshold && u_new >= a.act_threshold) {
-        const int32_t t1 = (int32_t)a.t + 1;
+        const int32_t t1 = (int32_t)t + 1;
         a.act_last[off] = t1;
         if (a.act_first[off] < 0) a.act_first[off] = t1;
         a.act_count[off] += 1;
@@ -54,7 +54,8 @@ __device__ __forceinline__ void record_activation(const StepArgs &a, int64_t off
 }
 
 template <bool ACT>
-__device__ __noinline__ void boundary_cell(const StepArgs &a, unsigned active, bool deriv, int i, int j) {
+__device__ __noinline__ void boundary_cell(const StepArgs &a, float t, unsigned active, bool deriv,
+                                           int i, int j) {
     const Clamped U{a.u, a.H, a.W, a.pitch}, D{a.D, a.H, a.W, a.pitch};
     const int H = a.H, W = a.W;
     const float rdx = a.rdx;
@@ -103,7 +104,7 @@ __device__ __noinline__ void boundary_cell(const StepArgs &a, unsigned active, b
         a.wo[off] = fmaf(r.dw, a.dt, w);
         const float un = fmaf(du, a.dt, u);
         a.uo[off] = un;
-        if (ACT) record_activation(a, off, u, un);
+        if (ACT) record_activation(a, t, off, u, un);
     }
 }
 
@@ -134,8 +135,8 @@ __device__ __noinline__ float4 apply_stimuli(const StepArgs &a, unsigned active,
 // Cells of tile (i0, j0) within BAND of an edge, enumerated compactly so that each thread
 // takes ceil(count / NT) of them: a top strip, a bottom strip, and left/right strips between.
 template <bool ACT>
-__device__ __noinline__ void boundary_band(const StepArgs &a, unsigned active, bool deriv, int i0,
-                                           int j0) {
+__device__ __noinline__ void boundary_band(const StepArgs &a, float t, unsigned active, bool deriv,
+                                           int i0, int j0) {
     const int H = a.H, W = a.W;
     const int i1 = min(i0 + TY, H), j1 = min(j0 + TX, W);
     const int jw = j1 - j0;
@@ -160,7 +161,7 @@ __device__ __noinline__ void boundary_band(const StepArgs &a, unsigned active, b
             i = ri0 + r;
             j = c < wl ? j0 + c : rj1 + (c - wl);
         }
-        boundary_cell<ACT>(a, active, deriv, i, j);
+        boundary_cell<ACT>(a, t, active, deriv, i, j);
     }
 }
 
@@ -194,8 +195,9 @@ __device__ __forceinline__ void issue_tile(const StepMaps &tm, const Stage &st, 
 // One tile: pass 1 (first derivatives into shared memory), pass 2 (everything else), and the
 // boundary band of edge tiles.
 template <bool DERIV, bool ACT>
-__device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage &st, float *sux,
-                                             float *suy, unsigned active, int i0, int j0) {
+__device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const Stage &st,
+                                             float *sux, float *suy, unsigned active, int i0,
+                                             int j0) {
     const int tid = threadIdx.x;
     const int H = a.H, W = a.W, pitch = a.pitch;
     const float rdx = a.rdx;
@@ -300,7 +302,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage &st,
             st4(a.uo + goff, make_float4(ou[0], ou[1], ou[2], ou[3]));
             if (ACT && !DERIV) {
 #pragma unroll
-                for (int m = 0; m < 4; ++m) record_activation(a, goff + m, uu[m], ou[m]);
+                for (int m = 0; m < 4; ++m) record_activation(a, t, goff + m, uu[m], ou[m]);
             }
         } else if (i >= BAND && i < H - BAND) {
 #pragma unroll
@@ -310,12 +312,21 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const Stage &st,
                     a.vo[goff + m] = ov[m];
                     a.wo[goff + m] = ow[m];
                     a.uo[goff + m] = ou[m];
-                    if (ACT && !DERIV) record_activation(a, goff + m, uu[m], ou[m]);
+                    if (ACT && !DERIV) record_activation(a, t, goff + m, uu[m], ou[m]);
                 }
             }
         }
     }
-    if (!interior) boundary_band<ACT && !DERIV>(a, active, DERIV, i0, j0);
+    if (!interior) boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0);
+}
+
+static_assert(sizeof(StepArgs) <= SMEM_ARGS_BYTES, "StepArgs does not fit its shared slot");
+
+// Copies a StepArgs into shared memory (all threads; a barrier must follow).
+__device__ __forceinline__ void stage_args(StepArgs *dst, const StepArgs *src) {
+    const uint32_t *s = reinterpret_cast<const uint32_t *>(src);
+    uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(StepArgs) / 4); k += NT) d[k] = s[k];
 }
 
 // ---- the step kernel: persistent CTAs over the tiles of one tissue ------------------------
@@ -328,9 +339,11 @@ __global__ void __launch_bounds__(NT, 1) fk_step_kernel(const __grid_constant__ 
     float *sux = reinterpret_cast<float *>(smem + 2 * SMEM_STAGE_BYTES);  // [SUX_H][TX]
     float *suy = sux + TX * SUX_H;                                          // [TY][SW]
     uint64_t *bar = reinterpret_cast<uint64_t *>(suy + SW * TY);            // [2]
+    StepArgs *sa = reinterpret_cast<StepArgs *>(bar + 2);
 
     const int tid = threadIdx.x;
     const int ntx = (a.W + TX - 1) / TX, nty = (a.H + TY - 1) / TY, ntiles = ntx * nty;
+    stage_args(sa, &a);
     if (tid == 0) {
         prefetch_tensormap(&tm.u);
         prefetch_tensormap(&tm.v);
@@ -360,10 +373,114 @@ __global__ void __launch_bounds__(NT, 1) fk_step_kernel(const __grid_constant__ 
             if (tid == 0) atomicOr(a.status, kStatusTimeout);
             return;
         }
-        compute_tile<DERIV, ACT>(a, stage_at(smem, s), sux, suy, active, (tile / ntx) * TY,
+        compute_tile<DERIV, ACT>(*sa, a.t, stage_at(smem, s), sux, suy, active, (tile / ntx) * TY,
                                  (tile % ntx) * TX);
         __syncthreads();  // stage s and the u_x/u_y buffers are free again
     }
+}
+
+// ---- batched kernel: persistent CTAs over the tiles of many tissues ------------------------
+template <bool ACT>
+__global__ void __launch_bounds__(NT, 1)
+    fk_batch_kernel(const BatchTissue *__restrict__ tissues, const BatchMaps *__restrict__ maps,
+                    const BatchItem *__restrict__ items, int n_items, const int *t_dev,
+                    int t_offset, int parity, int *status) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    float *sux = reinterpret_cast<float *>(smem + 2 * SMEM_STAGE_BYTES);
+    float *suy = sux + TX * SUX_H;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(suy + SW * TY);
+    StepArgs *sa = reinterpret_cast<StepArgs *>(bar + 2);  // arguments of the current tile's tissue
+
+    const int tid = threadIdx.x;
+    const float t = (float)(*t_dev + t_offset);
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    int it = blockIdx.x;
+    if (tid == 0 && it < n_items) {
+        const BatchItem b = items[it];
+        issue_tile(maps[b.tissue].maps[parity], stage_at(smem, 0), &bar[0], b.i0, b.j0);
+    }
+    for (int n = 0; it < n_items; ++n, it += gridDim.x) {
+        const int s = n & 1;
+        const int next = it + gridDim.x;
+        if (tid == 0 && next < n_items) {
+            const BatchItem b = items[next];
+            issue_tile(maps[b.tissue].maps[parity], stage_at(smem, s ^ 1), &bar[s ^ 1], b.i0, b.j0);
+        }
+        const BatchItem b = items[it];
+        stage_args(sa, &tissues[b.tissue].args[parity]);  // this tissue's arguments
+        const bool ok = mbar_wait_bounded(&bar[s], (n >> 1) & 1);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(status, kStatusTimeout);
+            return;
+        }
+        unsigned active = 0;
+        for (int k = 0; k < sa->n_stim; ++k)
+            if (stim_active(sa->stim[k], t)) active |= 1u << k;
+        compute_tile<false, ACT>(*sa, t, stage_at(smem, s), sux, suy, active, b.i0, b.j0);
+        __syncthreads();
+    }
+}
+
+__global__ void add_int_kernel(int *p, int v) { *p += v; }
+
+__global__ void batch_copyback_kernel(const BatchTissue *tissues) {
+    const StepArgs &src = tissues[blockIdx.y].args[1];   // reads scratch ...
+    const StepArgs &dst = tissues[blockIdx.y].args[0];   // ... into state
+    const int64_t plane = (int64_t)src.H * src.pitch;
+    const float *in[3] = {src.v, src.w, src.u};
+    float *out[3] = {const_cast<float *>(dst.v), const_cast<float *>(dst.w),
+                     const_cast<float *>(dst.u)};
+    for (int p = 0; p < 3; ++p)
+        for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < plane;
+             k += (int64_t)gridDim.x * blockDim.x)
+            out[p][k] = in[p][k];
+}
+
+cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
+                              const BatchItem *items, int n_items, const int *t_dev, int t_offset,
+                              int parity, bool act, int *status, int grid, cudaStream_t stream) {
+    static thread_local int configured_device = -1;
+    int dev = -1;
+    cudaGetDevice(&dev);
+    if (dev != configured_device) {
+        cudaError_t e;
+        if ((e = cudaFuncSetAttribute(fk_batch_kernel<true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      SMEM_BATCH_BYTES)) != cudaSuccess)
+            return e;
+        if ((e = cudaFuncSetAttribute(fk_batch_kernel<false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      SMEM_BATCH_BYTES)) != cudaSuccess)
+            return e;
+        configured_device = dev;
+    }
+    if (grid > n_items) grid = n_items;
+    if (grid < 1) return cudaSuccess;
+    if (act)
+        fk_batch_kernel<true><<<grid, NT, SMEM_BATCH_BYTES, stream>>>(tissues, maps, items, n_items,
+                                                                       t_dev, t_offset, parity, status);
+    else
+        fk_batch_kernel<false><<<grid, NT, SMEM_BATCH_BYTES, stream>>>(tissues, maps, items, n_items,
+                                                                        t_dev, t_offset, parity, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_int(int *p, int v, cudaStream_t stream) {
+    add_int_kernel<<<1, 1, 0, stream>>>(p, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_copyback(const BatchTissue *tissues, int n_tissues, cudaStream_t stream) {
+    if (n_tissues < 1) return cudaSuccess;
+    batch_copyback_kernel<<<dim3(64, n_tissues), 256, 0, stream>>>(tissues);
+    return cudaGetLastError();
 }
 
 template <bool DERIV, bool ACT>

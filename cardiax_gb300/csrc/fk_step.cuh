@@ -30,8 +30,9 @@ constexpr int SMEM_VW_BYTES = TX * TY * 4;  // one of the v, w tiles (no halo)
 constexpr int SMEM_STAGE_BYTES = SMEM_U_BYTES + SMEM_D_BYTES + 2 * SMEM_VW_BYTES;
 constexpr int SMEM_UX_BYTES = TX * SUX_H * 4;
 constexpr int SMEM_UY_BYTES = SW * TY * 4;
-constexpr int SMEM_STEP_BYTES =
-    2 * SMEM_STAGE_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES + 16 + 128;  // + 2 mbarriers + align
+constexpr int SMEM_ARGS_BYTES = 1024;  // staged StepArgs (static_assert in fk_step.cu)
+constexpr int SMEM_STEP_BYTES = 2 * SMEM_STAGE_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES + 16 +
+                                SMEM_ARGS_BYTES + 128;  // + 2 mbarriers + args + align
 // Cells within this distance of an edge take the per-cell boundary path (one-sided stencils
 // and edge padding reach 4 cells in).
 constexpr int BAND = 4;
@@ -65,5 +66,31 @@ struct StepMaps {
 // above it during step t -> t+1 gets act_last = t+1, act_first = t+1 if it was -1, and
 // act_count + 1.
 cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream);
+
+// ---- batched tissues ------------------------------------------------------------------------
+// Device-resident descriptors of one tissue in a batch: the step arguments and TMA maps for
+// both ping-pong parities (parity p reads buffer p: 0 = state, 1 = scratch).
+struct BatchTissue {
+    StepArgs args[2];
+};
+struct BatchMaps {
+    StepMaps maps[2];
+};
+// One unit of the work list: a TY x TX tile of one tissue.
+struct BatchItem {
+    int32_t tissue, i0, j0, pad;
+};
+
+constexpr int SMEM_BATCH_BYTES = SMEM_STEP_BYTES;
+
+// One Euler step of every tissue: persistent CTAs drain `items`; the step index is
+// *t_dev + t_offset (so that a captured graph can be replayed for successive steps).
+cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
+                              const BatchItem *items, int n_items, const int *t_dev, int t_offset,
+                              int parity, bool act, int *status, int grid, cudaStream_t stream);
+// *p += v (advances the step counter of a captured graph).
+cudaError_t launch_add_int(int *p, int v, cudaStream_t stream);
+// Copies buffer 1 (scratch) of every tissue back to buffer 0 (state).
+cudaError_t launch_batch_copyback(const BatchTissue *tissues, int n_tissues, cudaStream_t stream);
 
 }  // namespace fk

@@ -117,6 +117,44 @@ int fk_forward_euler_tracked(fk_grid g, float *state, float *scratch, const floa
                              int64_t t0, int64_t t1, double dt, double dx,
                              const fk_activation *act, void *stream);
 
+/* ---- many tissues in one launch --------------------------------------------------------------
+ * No reference counterpart: the reference steps one tissue per call (its data generation loops
+ * over tissues in Python, deepx/generate.py:135-210).  Here every tissue of a batch advances in
+ * one persistent kernel per step that drains a list of 32x128 tiles of all tissues, and runs of
+ * steps are replayed from a captured CUDA graph.  Tissues may differ in shape, parameters, D,
+ * stimuli and dt/dx; they advance through the same step indices. */
+typedef struct {
+    fk_grid g;
+    float *state;   /* (3, H, pitch), advanced in place                      */
+    float *scratch; /* (3, H, pitch), ping-pong buffer                       */
+    const float *D;
+    fk_params params;
+    const fk_stimulus *stimuli; /* copied at fk_batch_create             */
+    int n_stimuli;
+    double dt, dx;
+    fk_activation act; /* act.last == NULL: no activation tracking       */
+} fk_tissue;
+
+typedef struct fk_batch fk_batch; /* opaque host-side plan */
+
+/* Device workspace (bytes) that fk_batch_create needs for these tissues. */
+size_t fk_batch_workspace_bytes(const fk_tissue *tissues, int n_tissues);
+
+/* Validates the tissues, writes their descriptors, TMA maps and the tile list into `workspace`
+ * (device memory of at least fk_batch_workspace_bytes, 128-byte aligned) on `stream`, and
+ * returns a host-side plan.  The tissues' buffers must outlive the plan. */
+int fk_batch_create(const fk_tissue *tissues, int n_tissues, void *workspace,
+                    size_t workspace_bytes, void *stream, fk_batch **plan);
+
+/* Advances every tissue through steps t0 .. t1-1.  graph_steps > 0 captures that many steps
+ * (rounded up to even) into a CUDA graph once per plan and replays it; 0 launches each step. */
+int fk_batch_forward_euler(fk_batch *plan, int64_t t0, int64_t t1, int graph_steps, void *stream);
+
+/* Number of persistent CTAs per launch (default: one per SM); a tuning knob. */
+int fk_batch_set_grid(fk_batch *plan, int ctas);
+
+int fk_batch_destroy(fk_batch *plan);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,85 @@
+"""The batched path (one persistent kernel per step over all tissues, CUDA-graph replay) against
+the single-tissue path: every tissue must come out bit-identical."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _mixed_tissues(rng, track=False):
+    from cardiax_gb300 import params as Pm
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    from cardiax_gb300.tissue import Tissue
+    shapes = [(64, 64), (128, 128), (37, 90), (256, 130), (3, 5), (200, 64), (96, 257)]
+    sets = [Pm.PARAMSET_1A, Pm.PARAMSET_3, Pm.PARAMSET_4A, Pm.PARAMSET_5]
+    out = []
+    for k, (H, W) in enumerate(shapes):
+        i, j = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+        D = (1e-3 * (1 - 0.7 * np.exp(-((i - H * rng.uniform()) ** 2 + (j - W * rng.uniform()) ** 2)
+                                      / (0.05 * H * W + 1)))).astype(np.float32)
+        f = np.zeros((H, W), np.float32)
+        if k % 2:
+            f[:, : max(1, W // 10)] = 20.0
+        else:
+            r, c = rng.integers(0, max(1, H - 10)), rng.integers(0, max(1, W - 10))
+            f[r:r + 10, c:c + 10] = 20.0
+        proto = Protocol(int(rng.integers(0, 20)), 2, int(rng.integers(150, 400)))
+        t = Tissue((H, W), sets[k % 4], D, [Stimulus(proto, f)], dt=0.01, dx=0.01)
+        if track:
+            t.track_activation(0.5)
+        out.append(t)
+    return out
+
+
+@pytest.mark.parametrize("graph_steps,n_steps", [(0, 37), (16, 101), (64, 64)])
+def test_batch_matches_single_tissue_bitwise(graph_steps, n_steps):
+    _gpu()
+    from cardiax_gb300.batch import TissueBatch
+    a = _mixed_tissues(np.random.default_rng(1))
+    b = _mixed_tissues(np.random.default_rng(1))
+    for t in a:
+        t.advance(0, n_steps)
+    batch = TissueBatch(b, graph_steps=graph_steps)
+    batch.advance(0, n_steps)
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        for p, q in zip(x.view(), y.view()):
+            assert torch.equal(p, q), (x.H, x.W)
+    batch.close()
+
+
+def test_batch_continues_across_calls_and_tracks_activation():
+    _gpu()
+    from cardiax_gb300.batch import TissueBatch
+    a = _mixed_tissues(np.random.default_rng(2), track=True)
+    b = _mixed_tissues(np.random.default_rng(2), track=True)
+    for t in a:
+        t.advance(0, 500)
+    batch = TissueBatch(b, graph_steps=32)
+    batch.advance(0, 123).advance(123, 500)
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        for p, q in zip(x.view(), y.view()):
+            assert torch.equal(p, q)
+        for p, q in zip(x.activation_maps(), y.activation_maps()):
+            assert torch.equal(p, q)
+    assert any(int((t.activation_maps()[0] >= 0).sum()) > 0 for t in b)
+
+
+def test_autotuner_restores_state_and_picks_a_candidate():
+    _gpu()
+    from cardiax_gb300.autotune import tune_batch
+    from cardiax_gb300.batch import TissueBatch
+    b = _mixed_tissues(np.random.default_rng(3))
+    before = [t.state.clone() for t in b]
+    batch = TissueBatch(b)
+    res = tune_batch(batch, trial_steps=32, candidates=(0, 16))
+    assert res["graph_steps"] in (0, 16)
+    for t, s in zip(b, before):
+        assert torch.equal(t.state, s)

@@ -268,7 +268,7 @@ def test_activation_times_within_one_step():
     tis = Tissue((H, W), P3, D, [Stimulus(Protocol(*s[:3]), s[3]) for s in stims])
     tis.track_activation(0.5).advance(0, 6000)
     gf, gl, gc = (_np(x) for x in tis.activation_maps())
-    assert (first >= 0).mean() > 0.9  # the wave reached most of the tissue
+    assert (first >= 0).mean() > 0.8  # the wave reached most of the tissue
     assert np.array_equal(gf >= 0, first >= 0)
     assert np.abs(gf - first).max() <= 1
     assert np.abs(gl - last).max() <= 1
