@@ -1,0 +1,170 @@
+"""Reverse mode through the stepper: adjoint Euler steps with sqrt(T) checkpoint-and-recompute,
+exposed as a ``torch.autograd.Function``.
+
+The reference never differentiates its stepper; this provides the derivative that ``jax.grad``
+of a scan over ``cardiax.solve.step_euler`` (cardiax/solve.py:68-70) defines, with the Heaviside
+gates and the stimulus replacement contributing zero derivative.  Gradients are taken with
+respect to the initial state, the per-cell diffusivity D and the first 13 fields of ``Params``
+(``Cm`` is held fixed).
+
+Memory: a rollout of T steps keeps ceil(T / K) checkpoints plus one segment of K recomputed
+states, K = ceil(sqrt(T)) by default (e.g. 1e4 steps at 512^2: 200 states of 3 MiB).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Sequence
+
+import torch
+
+from . import _native as N
+from .tissue import Tissue, as_cuda_f32, stream_handle
+
+N_THETA = 13
+
+
+def _lib():
+    L = N.lib()
+    if not getattr(L, "_adjoint_bound", False):
+        L.fk_adjoint_slots.restype = ctypes.c_int64
+        L.fk_adjoint_slots.argtypes = [N.Grid]
+        L.fk_adjoint_step.restype = ctypes.c_int
+        L.fk_adjoint_step.argtypes = [N.Grid, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.POINTER(N.Params), ctypes.POINTER(N.Stimulus),
+                                      ctypes.c_int, ctypes.c_int64, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L._adjoint_bound = True
+    return L
+
+
+class Adjoint:
+    """Reverse-mode helper bound to one :class:`Tissue` (its D, parameters and stimuli)."""
+
+    def __init__(self, tissue: Tissue):
+        self.t = tissue
+        L = _lib()
+        self.slots = int(L.fk_adjoint_slots(tissue.grid))
+        dev = tissue.device
+        self.gD = torch.zeros((tissue.H, tissue.pitch), dtype=torch.float32, device=dev)
+        self.gtheta = torch.zeros((self.slots, 16), dtype=torch.float64, device=dev)
+
+    def zero_grad(self):
+        self.gD.zero_()
+        self.gtheta.zero_()
+
+    def step(self, state: torch.Tensor, t: int, lam_next: torch.Tensor, lam: torch.Tensor):
+        """lam <- cotangent of x_t given the cotangent lam_next of x_{t+1}; accumulates dL/dD
+        and dL/dtheta."""
+        T = self.t
+        rc = _lib().fk_adjoint_step(T.grid, state.data_ptr(), T.D.data_ptr(),
+                                    ctypes.byref(T.params), T.stim, T.n_stim, int(t), T.dt, T.dx,
+                                    lam_next.data_ptr(), lam.data_ptr(), self.gD.data_ptr(),
+                                    self.gtheta.data_ptr(), stream_handle())
+        if rc:
+            raise N.FkError(rc, "fk_adjoint_step")
+
+    def grad_theta(self) -> torch.Tensor:
+        """dL/dtheta (13 values, cardiax Params order), summed over the slots in index order."""
+        return self.gtheta[:, :N_THETA].sum(0)
+
+    def grad_D(self) -> torch.Tensor:
+        return self.gD[:, :self.t.W]
+
+    # -- rollouts -----------------------------------------------------------------------------
+    def rollout_gradient(self, state0: torch.Tensor, t0: int, t1: int, obs_times: Sequence[int],
+                         obs_grads: torch.Tensor, seg: int = None) -> torch.Tensor:
+        """Backward pass of a rollout from ``state0`` ((3, H, pitch)) over steps t0 .. t1-1,
+        where the loss depends on the states at ``obs_times`` (each in [t0, t1]) with
+        dL/dx_{obs_times[k]} = obs_grads[k] ((n_obs, 3, H, pitch)).  Returns dL/dx_{t0};
+        dL/dD and dL/dtheta accumulate in this object.  Uses checkpoints every ``seg`` steps
+        (default ceil(sqrt(T))) and recomputes one segment at a time."""
+        T = self.t
+        n = t1 - t0
+        seg = seg or max(1, math.ceil(math.sqrt(max(n, 1))))
+        obs_index = {}
+        for k, tt in enumerate(obs_times):
+            obs_index.setdefault(int(tt), []).append(k)
+        # forward: checkpoints at t0, t0+seg, ...
+        ckpts = []
+        T.state.copy_(state0)
+        for s in range(t0, t1, seg):
+            ckpts.append((s, T.state.clone()))
+            T.advance(s, min(s + seg, t1))
+        lam = torch.zeros_like(state0)
+        lam_tmp = torch.empty_like(state0)
+        if t1 in obs_index:
+            for k in obs_index[t1]:
+                lam += obs_grads[k]
+        buf = torch.empty((seg,) + tuple(state0.shape), dtype=state0.dtype, device=state0.device)
+        for s, st in reversed(ckpts):
+            e = min(s + seg, t1)
+            # recompute x_s .. x_{e-1} into buf
+            buf[0].copy_(st)
+            for k in range(1, e - s):
+                N.call("fk_euler_step", T.grid, buf[k - 1].data_ptr(), T.D.data_ptr(),
+                       ctypes.byref(T.params), T.stim, T.n_stim, s + k - 1, T.dt, T.dx,
+                       buf[k].data_ptr(), stream_handle())
+            for tt in range(e - 1, s - 1, -1):
+                self.step(buf[tt - s], tt, lam, lam_tmp)
+                lam, lam_tmp = lam_tmp, lam
+                if tt in obs_index:
+                    for k in obs_index[tt]:
+                        lam += obs_grads[k]
+        return lam
+
+
+class _Rollout(torch.autograd.Function):
+    """States at ``obs_times`` of a rollout, differentiable w.r.t. (v0, w0, u0, D, theta)."""
+
+    @staticmethod
+    def forward(ctx, v0, w0, u0, D, theta, Cm, stimuli, t0, t1, obs_times, dt, dx, seg):
+        params = [float(x) for x in theta.detach().cpu().tolist()] + [float(Cm)]
+        H, W = u0.shape
+        tis = Tissue((H, W), params, D.detach(), stimuli, dt=dt, dx=dx, device=u0.device)
+        tis.set_state((v0.detach(), w0.detach(), u0.detach()))
+        state0 = tis.state.clone()
+        obs = sorted(set(int(t) for t in obs_times))
+        out = torch.empty((len(obs_times), 3, H, W), dtype=torch.float32, device=u0.device)
+        cur = t0
+        snaps = {}
+        if t0 in obs:
+            snaps[t0] = tis.state[:, :, :W].clone()
+        for t in obs:
+            if t <= cur:
+                continue
+            tis.advance(cur, t)
+            cur = t
+            snaps[t] = tis.state[:, :, :W].clone()
+        for k, t in enumerate(obs_times):
+            out[k] = snaps[int(t)]
+        ctx.save_for_backward(state0)
+        ctx.tis, ctx.t0, ctx.t1, ctx.obs_times, ctx.seg, ctx.W = tis, t0, t1, list(obs_times), seg, W
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (state0,) = ctx.saved_tensors
+        tis, W = ctx.tis, ctx.W
+        adj = Adjoint(tis)
+        g = torch.zeros((len(ctx.obs_times),) + tuple(state0.shape), dtype=torch.float32,
+                        device=state0.device)
+        g[..., :W] = grad_out.to(torch.float32)
+        t_end = max([ctx.t0] + [int(t) for t in ctx.obs_times])
+        lam0 = adj.rollout_gradient(state0, ctx.t0, t_end, ctx.obs_times, g, seg=ctx.seg)
+        gth = adj.grad_theta().to(torch.float32)
+        return (lam0[0, :, :W], lam0[1, :, :W], lam0[2, :, :W], adj.grad_D().clone(), gth,
+                None, None, None, None, None, None, None, None)
+
+
+def rollout(v0, w0, u0, D, theta, stimuli, t0: int, t1: int, obs_times: Sequence[int],
+            dt: float = 0.01, dx: float = 0.01, Cm: float = 1.0, seg: int = None):
+    """Differentiable rollout: the states (n_obs, 3, H, W) at ``obs_times`` (steps in
+    [t0, t1]) starting from (v0, w0, u0) at step t0.  Gradients flow to v0, w0, u0, D and
+    ``theta`` (the 13 first Params fields) through the hand-written adjoint kernel with
+    sqrt(T) checkpointing."""
+    dev = u0.device if isinstance(u0, torch.Tensor) and u0.is_cuda else torch.device("cuda")
+    to = lambda x: x if isinstance(x, torch.Tensor) and x.is_cuda else as_cuda_f32(x, dev)  # noqa: E731
+    return _Rollout.apply(to(v0), to(w0), to(u0), to(D), to(theta), Cm, list(stimuli), int(t0),
+                          int(t1), list(obs_times), float(dt), float(dx), seg)

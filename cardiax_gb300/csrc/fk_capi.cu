@@ -129,30 +129,45 @@ int make_stims(const fk_stimulus *s, int n, const fk_grid &g, Stim *out) {
 }
 
 // TMA descriptors of the state buffers seen by one call (the ping-pong buffers and checkpoint
-// slots): u with its halo box, v and w with the plain tile box.
+// slots): u with its halo box, v and w with the plain tile box, and u with the tile box (for
+// the stores of a step that writes this buffer).
 struct MapCache {
-    const float *ptr[4] = {nullptr, nullptr, nullptr, nullptr};
-    CUtensorMap u[4], v[4], w[4];
+    static constexpr int kSlots = 4;
+    const float *ptr[kSlots] = {nullptr, nullptr, nullptr, nullptr};
+    CUtensorMap u[kSlots], v[kSlots], w[kSlots], ut[kSlots];
     int next = 0;
-    int get(const fk_grid &g, const float *state, StepMaps &out) {
+    // slot of `state`, building its maps if needed without evicting slot `keep`
+    int lookup(const fk_grid &g, const float *state, int keep, int *slot) {
+        for (int i = 0; i < kSlots; ++i)
+            if (ptr[i] == state) {
+                *slot = i;
+                return FK_OK;
+            }
+        int k = next;
+        if (k == keep) k = (k + 1) % kSlots;
+        next = (k + 1) % kSlots;
         const int64_t plane = g.H * g.pitch;
-        int k = -1;
-        for (int i = 0; i < 4; ++i)
-            if (ptr[i] == state) k = i;
-        if (k < 0) {
-            k = next;
-            next = (next + 1) & 3;
-            int rc;
-            ptr[k] = nullptr;
-            if ((rc = make_plane_map(&u[k], state + 2 * plane, g.H, g.W, g.pitch, SW, SU_H)) ||
-                (rc = make_plane_map(&v[k], state, g.H, g.W, g.pitch, TX, TY)) ||
-                (rc = make_plane_map(&w[k], state + plane, g.H, g.W, g.pitch, TX, TY)))
-                return rc;
-            ptr[k] = state;
-        }
-        out.u = u[k];
-        out.v = v[k];
-        out.w = w[k];
+        int rc;
+        ptr[k] = nullptr;
+        if ((rc = make_plane_map(&u[k], state + 2 * plane, g.H, g.W, g.pitch, SW, SU_H)) ||
+            (rc = make_plane_map(&v[k], state, g.H, g.W, g.pitch, TX, TY)) ||
+            (rc = make_plane_map(&w[k], state + plane, g.H, g.W, g.pitch, TX, TY)) ||
+            (rc = make_plane_map(&ut[k], state + 2 * plane, g.H, g.W, g.pitch, TX, TY)))
+            return rc;
+        ptr[k] = state;
+        *slot = k;
+        return FK_OK;
+    }
+    // maps of a step reading `in` and writing `out`
+    int get(const fk_grid &g, const float *in, const float *out, StepMaps &sm) {
+        int ki, ko, rc;
+        if ((rc = lookup(g, in, -1, &ki)) || (rc = lookup(g, out, ki, &ko))) return rc;
+        sm.u = u[ki];
+        sm.v = v[ki];
+        sm.w = w[ki];
+        sm.ov = v[ko];
+        sm.ow = w[ko];
+        sm.ou = ut[ko];
         return FK_OK;
     }
 };
@@ -164,7 +179,7 @@ int step_once(const fk_grid &g, const float *in, float *out, const float *D, con
               const fk_activation *act = nullptr) {
     const int64_t plane = g.H * g.pitch;
     StepMaps sm;
-    int rc = maps.get(g, in, sm);
+    int rc = maps.get(g, in, out, sm);
     if (rc) return rc;
     sm.d = tm_d;
     StepArgs a{};

@@ -53,9 +53,15 @@ __device__ __forceinline__ void record_activation(const StepArgs &a, float t, in
     }
 }
 
+// Output tile in shared memory (dense TY x TX per plane) that the TMA stores write out.
+struct OutTile {
+    float *v, *w, *u;
+    int i0, j0;
+};
+
 template <bool ACT>
 __device__ __noinline__ void boundary_cell(const StepArgs &a, float t, unsigned active, bool deriv,
-                                           int i, int j) {
+                                           int i, int j, const OutTile &o) {
     const Clamped U{a.u, a.H, a.W, a.pitch}, D{a.D, a.H, a.W, a.pitch};
     const int H = a.H, W = a.W;
     const float rdx = a.rdx;
@@ -95,15 +101,16 @@ __device__ __noinline__ void boundary_cell(const StepArgs &a, float t, unsigned 
         if (acc != 0.0f) r.j_ion = acc;
     }
     const float du = diffusion(d, dxD, dyD, UX(i), UY(j), uxx, uyy) + r.j_ion;
+    const int lo = (i - o.i0) * TX + (j - o.j0);
     if (deriv) {
-        a.vo[off] = r.dv;
-        a.wo[off] = r.dw;
-        a.uo[off] = du;
+        o.v[lo] = r.dv;
+        o.w[lo] = r.dw;
+        o.u[lo] = du;
     } else {
-        a.vo[off] = fmaf(r.dv, a.dt, v);
-        a.wo[off] = fmaf(r.dw, a.dt, w);
+        o.v[lo] = fmaf(r.dv, a.dt, v);
+        o.w[lo] = fmaf(r.dw, a.dt, w);
         const float un = fmaf(du, a.dt, u);
-        a.uo[off] = un;
+        o.u[lo] = un;
         if (ACT) record_activation(a, t, off, u, un);
     }
 }
@@ -136,7 +143,7 @@ __device__ __noinline__ float4 apply_stimuli(const StepArgs &a, unsigned active,
 // takes ceil(count / NT) of them: a top strip, a bottom strip, and left/right strips between.
 template <bool ACT>
 __device__ __noinline__ void boundary_band(const StepArgs &a, float t, unsigned active, bool deriv,
-                                           int i0, int j0) {
+                                           int i0, int j0, const OutTile &o) {
     const int H = a.H, W = a.W;
     const int i1 = min(i0 + TY, H), j1 = min(j0 + TX, W);
     const int jw = j1 - j0;
@@ -161,7 +168,7 @@ __device__ __noinline__ void boundary_band(const StepArgs &a, float t, unsigned 
             i = ri0 + r;
             j = c < wl ? j0 + c : rj1 + (c - wl);
         }
-        boundary_cell<ACT>(a, t, active, deriv, i, j);
+        boundary_cell<ACT>(a, t, active, deriv, i, j, o);
     }
 }
 
@@ -192,49 +199,121 @@ __device__ __forceinline__ void issue_tile(const StepMaps &tm, const Stage &st, 
     tma_load_2d(st.w, &tm.w, j0, i0, bar);
 }
 
-// One tile: pass 1 (first derivatives into shared memory), pass 2 (everything else), and the
-// boundary band of edge tiles.
-template <bool DERIV, bool ACT>
+// Edge tiles: replace the zero fill of out-of-grid halo cells by the reference's edge padding
+// (copies of the first/last row and column), so that the stencils read clamped values.
+__device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_rows, int i0, int j0, int H,
+                                        int W) {
+    const int tid = threadIdx.x;
+    // rows outside [0, H)
+    for (int it = tid; it < rows * SW; it += NT) {
+        const int sr = it / SW, c = it % SW;
+        const int gr = i0 - halo_rows + sr;
+        if (gr < 0 || gr >= H) {
+            const int src = (gr < 0 ? 0 : H - 1) - i0 + halo_rows;
+            buf[sr * SW + c] = buf[src * SW + c];
+        }
+    }
+    __syncthreads();
+    // columns outside [0, W)
+    for (int it = tid; it < rows * SW; it += NT) {
+        const int sr = it / SW, c = it % SW;
+        const int gc = j0 - HALO_U + c;
+        if (gc < 0 || gc >= W) {
+            const int src = (gc < 0 ? 0 : W - 1) - j0 + HALO_U;
+            buf[sr * SW + c] = buf[sr * SW + src];
+        }
+    }
+}
+
+// One tile: pass 1 (first derivatives into shared memory), pass 2 (everything else).
+// EDGE: the tile touches the grid edge (and is not a one-row or one-column sliver): the halo
+// is clamped and every derivative picks the reference's row type, exactly as the padded
+// arrays of cardiax/solve.py:29-32,49-54 do.
+template <bool DERIV, bool ACT, bool EDGE>
 __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const Stage &st,
-                                             float *sux, float *suy, unsigned active, int i0,
-                                             int j0) {
+                                             float *sux, float *suy, float *sou, unsigned active,
+                                             int i0, int j0) {
     const int tid = threadIdx.x;
     const int H = a.H, W = a.W, pitch = a.pitch;
     const float rdx = a.rdx;
-    const float *su = st.u, *sd = st.d;
+    float *su = st.u, *sd = st.d;
+
+    if (EDGE) {
+        clamp_halo(su, SU_H, HALO_U, i0, j0, H, W);
+        clamp_halo(sd, SD_H, HALO_D, i0, j0, H, W);
+        __syncthreads();
+    }
 
     // ---- pass 1: u_x (tile rows -2 .. TY+1) and u_y (tile columns -2 .. TX+1) -------------
 #pragma unroll 1
     for (int it = tid; it < SUX_H * NTX; it += NT) {
         const int r = it / NTX, q = it % NTX;
-        const float *b = su + (r + 2) * SW + HALO_U + 4 * q;
-        st4(sux + r * TX + 4 * q,
-            mul4(g_central4(ld4(b - 2 * SW), ld4(b - SW), ld4(b + SW), ld4(b + 2 * SW)), rdx));
+        const float *b = su + (r + 2) * SW + HALO_U + 4 * q;  // u row of ux row r
+        float4 o;
+        if (!EDGE) {
+            o = g_central4(ld4(b - 2 * SW), ld4(b - SW), ld4(b + SW), ld4(b + 2 * SW));
+        } else {
+            const int x = i0 - 2 + r;  // global row of this u_x row
+            if (x <= 0)
+                o = [&] {
+                    const float4 a0 = ld4(b), a1 = ld4(b + SW), a2 = ld4(b + 2 * SW), a3 = ld4(b + 3 * SW);
+                    return make_float4(g_head(a0.x, a1.x, a2.x, a3.x), g_head(a0.y, a1.y, a2.y, a3.y),
+                                       g_head(a0.z, a1.z, a2.z, a3.z), g_head(a0.w, a1.w, a2.w, a3.w));
+                }();
+            else if (x >= H - 1)
+                o = [&] {
+                    const float4 a0 = ld4(b - 3 * SW), a1 = ld4(b - 2 * SW), a2 = ld4(b - SW), a3 = ld4(b);
+                    return make_float4(g_tail(a0.x, a1.x, a2.x, a3.x), g_tail(a0.y, a1.y, a2.y, a3.y),
+                                       g_tail(a0.z, a1.z, a2.z, a3.z), g_tail(a0.w, a1.w, a2.w, a3.w));
+                }();
+            else
+                o = g_central4(ld4(b - 2 * SW), ld4(b - SW), ld4(b + SW), ld4(b + 2 * SW));
+        }
+        st4(sux + r * TX + 4 * q, mul4(o, rdx));
     }
 #pragma unroll 1
     for (int it = tid; it < TY * NTX; it += NT) {
         const int r = it / NTX, q = it % NTX;
         const float *b = su + (r + HALO_U) * SW + 4 * q;  // columns j0+4q-4 .. j0+4q+7
         const float4 x0 = ld4(b), x1 = ld4(b + 4), x2 = ld4(b + 8);
-        float4 o;
-        o.x = g_central(x0.z, x0.w, x1.y, x1.z) * rdx;
-        o.y = g_central(x0.w, x1.x, x1.z, x1.w) * rdx;
-        o.z = g_central(x1.x, x1.y, x1.w, x2.x) * rdx;
-        o.w = g_central(x1.y, x1.z, x2.x, x2.y) * rdx;
-        st4(suy + r * SW + HALO_U + 4 * q, o);
+        const float e[12] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
+                             x2.x, x2.y, x2.z, x2.w};
+        float o[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            if (!EDGE) {
+                o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
+            } else {  // u_y at padded position y: head / tail / central row of the padded line
+                const int y = j0 + 4 * q + m;
+                if (y <= 0) o[m] = g_head(e[m + 4], e[m + 5], e[m + 6], e[m + 7]);
+                else if (y >= W - 1) o[m] = g_tail(e[m + 1], e[m + 2], e[m + 3], e[m + 4]);
+                else o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
+            }
+        }
+        st4(suy + r * SW + HALO_U + 4 * q,
+            make_float4(o[0] * rdx, o[1] * rdx, o[2] * rdx, o[3] * rdx));
     }
-    if (tid < TY * 4) {  // the 2 + 2 halo columns of u_y
-        const int r = tid / 4, k = tid % 4;
+    if (tid >= NT - TY * 4) {  // the 2 + 2 halo columns of u_y (threads with one ux item less)
+        const int h = tid - (NT - TY * 4);
+        const int r = h / 4, k = h % 4;
         const int c = k < 2 ? 2 + k : TX + HALO_U + (k - 2);  // same column index in su and suy
         const float *row = su + (r + HALO_U) * SW;
-        suy[r * SW + c] = g_central(row[c - 2], row[c - 1], row[c + 1], row[c + 2]) * rdx;
+        float o;
+        if (!EDGE) {
+            o = g_central(row[c - 2], row[c - 1], row[c + 1], row[c + 2]);
+        } else {
+            const int y = j0 - HALO_U + c;
+            if (y <= 0) o = g_head(row[c], row[c + 1], row[c + 2], row[c + 3]);
+            else if (y >= W - 1) o = g_tail(row[c - 3], row[c - 2], row[c - 1], row[c]);
+            else o = g_central(row[c - 2], row[c - 1], row[c + 1], row[c + 2]);
+        }
+        suy[r * SW + c] = o * rdx;
     }
     __syncthreads();
 
     // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
     const int tx = tid % NTX, ty = tid / NTX;
     const int j = j0 + 4 * tx;
-    const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
 #pragma unroll 1
     for (int k = 0; k < RPT; ++k) {
         const int r = RPT * ty + k;
@@ -242,14 +321,31 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
         const int64_t goff = (int64_t)i * pitch + j;
         const float *xb = sux + (r + 2) * TX + 4 * tx;
         const float4 uxc = ld4(xb);
-        const float4 uxx = mul4(g_central4(ld4(xb - 2 * TX), ld4(xb - TX), ld4(xb + TX),
-                                           ld4(xb + 2 * TX)), rdx);
-        const float *yb = suy + r * SW + 4 * tx;
-        const float4 y0 = ld4(yb), y1 = ld4(yb + 4), y2 = ld4(yb + 8);
         const float *db = sd + (r + HALO_D) * SW + HALO_U + 4 * tx;
         const float4 dc = ld4(db);
-        const float4 dxD = mul4(g_central4(ld4(db - 2 * SW), ld4(db - SW), ld4(db + SW),
-                                           ld4(db + 2 * SW)), rdx);
+        float4 uxx, dxD;
+        if (!EDGE || (i != 0 && i != H - 1)) {
+            uxx = g_central4(ld4(xb - 2 * TX), ld4(xb - TX), ld4(xb + TX), ld4(xb + 2 * TX));
+            dxD = g_central4(ld4(db - 2 * SW), ld4(db - SW), ld4(db + SW), ld4(db + 2 * SW));
+        } else if (i == 0) {  // head rows on u_x rows 0..3 and D rows 0..3
+            const float4 a0 = uxc, a1 = ld4(xb + TX), a2 = ld4(xb + 2 * TX), a3 = ld4(xb + 3 * TX);
+            uxx = make_float4(g_head(a0.x, a1.x, a2.x, a3.x), g_head(a0.y, a1.y, a2.y, a3.y),
+                              g_head(a0.z, a1.z, a2.z, a3.z), g_head(a0.w, a1.w, a2.w, a3.w));
+            const float4 b0 = dc, b1 = ld4(db + SW), b2 = ld4(db + 2 * SW), b3 = ld4(db + 3 * SW);
+            dxD = make_float4(g_head(b0.x, b1.x, b2.x, b3.x), g_head(b0.y, b1.y, b2.y, b3.y),
+                              g_head(b0.z, b1.z, b2.z, b3.z), g_head(b0.w, b1.w, b2.w, b3.w));
+        } else {  // i == H-1: tail rows on rows H-4 .. H-1
+            const float4 a0 = ld4(xb - 3 * TX), a1 = ld4(xb - 2 * TX), a2 = ld4(xb - TX), a3 = uxc;
+            uxx = make_float4(g_tail(a0.x, a1.x, a2.x, a3.x), g_tail(a0.y, a1.y, a2.y, a3.y),
+                              g_tail(a0.z, a1.z, a2.z, a3.z), g_tail(a0.w, a1.w, a2.w, a3.w));
+            const float4 b0 = ld4(db - 3 * SW), b1 = ld4(db - 2 * SW), b2 = ld4(db - SW), b3 = dc;
+            dxD = make_float4(g_tail(b0.x, b1.x, b2.x, b3.x), g_tail(b0.y, b1.y, b2.y, b3.y),
+                              g_tail(b0.z, b1.z, b2.z, b3.z), g_tail(b0.w, b1.w, b2.w, b3.w));
+        }
+        uxx = mul4(uxx, rdx);
+        dxD = mul4(dxD, rdx);
+        const float *yb = suy + r * SW + 4 * tx;
+        const float4 y0 = ld4(yb), y1 = ld4(yb + 4), y2 = ld4(yb + 8);
         const float4 dl = ld4(db - 4), dr = ld4(db + 4);
         const float4 uc = ld4(su + (r + HALO_U) * SW + HALO_U + 4 * tx);
         const float4 vc = ld4(st.v + r * TX + 4 * tx), wc = ld4(st.w + r * TX + 4 * tx);
@@ -283,8 +379,25 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
         }
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            const float uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]) * rdx;
-            const float dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]) * rdx;
+            float uyy, dyD;
+            if (!EDGE) {
+                uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
+                dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
+            } else {  // second derivative / D_y at column y: head at 0, tail at W-1
+                const int y = j + m;
+                if (y == 0) {
+                    uyy = g_head(f[m + 4], f[m + 5], f[m + 6], f[m + 7]);
+                    dyD = g_head(g[m + 4], g[m + 5], g[m + 6], g[m + 7]);
+                } else if (y == W - 1) {
+                    uyy = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]);
+                    dyD = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]);
+                } else {
+                    uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
+                    dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
+                }
+            }
+            uyy *= rdx;
+            dyD *= rdx;
             const float du = diffusion(dd[m], dxv[m], dyD, uxv[m], f[m + 4], uxxv[m], uyy) + jion[m];
             if (DERIV) {
                 ov[m] = dv[m];
@@ -296,28 +409,62 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
                 ou[m] = fmaf(du, a.dt, uu[m]);
             }
         }
-        if (interior) {
-            st4(a.vo + goff, make_float4(ov[0], ov[1], ov[2], ov[3]));
-            st4(a.wo + goff, make_float4(ow[0], ow[1], ow[2], ow[3]));
-            st4(a.uo + goff, make_float4(ou[0], ou[1], ou[2], ou[3]));
-            if (ACT && !DERIV) {
+        // new v, w overwrite this thread's own cells of the stage; new u goes to sou
+        st4(st.v + r * TX + 4 * tx, make_float4(ov[0], ov[1], ov[2], ov[3]));
+        st4(st.w + r * TX + 4 * tx, make_float4(ow[0], ow[1], ow[2], ow[3]));
+        st4(sou + r * TX + 4 * tx, make_float4(ou[0], ou[1], ou[2], ou[3]));
+        if (ACT && !DERIV && i < H) {
 #pragma unroll
-                for (int m = 0; m < 4; ++m) record_activation(a, t, goff + m, uu[m], ou[m]);
-            }
-        } else if (i >= BAND && i < H - BAND) {
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                const int jj = j + m;
-                if (jj >= BAND && jj < W - BAND) {
-                    a.vo[goff + m] = ov[m];
-                    a.wo[goff + m] = ow[m];
-                    a.uo[goff + m] = ou[m];
-                    if (ACT && !DERIV) record_activation(a, t, goff + m, uu[m], ou[m]);
-                }
+            for (int m = 0; m < 4; ++m)
+                if (j + m < W) record_activation(a, t, goff + m, uu[m], ou[m]);
+        }
+    }
+}
+
+// A tile that needs the per-cell boundary path: the last row or column of tiles holds a
+// single grid row or column (too few rows in the tile for the one-sided stencils).
+__device__ __forceinline__ bool is_sliver(int i0, int j0, int H, int W) {
+    return H - i0 < 2 || W - j0 < 2;
+}
+
+// Interior tiles, clamped edge tiles, or slivers (interior passes + per-cell band).
+template <bool DERIV, bool ACT>
+__device__ __forceinline__ void process_tile(const StepArgs &a, float t, const Stage &st,
+                                             float *sux, float *suy, float *sou, unsigned active,
+                                             int i0, int j0) {
+    const int H = a.H, W = a.W;
+    const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
+    if (interior) {
+        compute_tile<DERIV, ACT, false>(a, t, st, sux, suy, sou, active, i0, j0);
+    } else if (!is_sliver(i0, j0, H, W)) {
+        compute_tile<DERIV, ACT, true>(a, t, st, sux, suy, sou, active, i0, j0);
+    } else {
+        compute_tile<DERIV, false, false>(a, t, st, sux, suy, sou, active, i0, j0);
+        __syncthreads();  // every cell of this tile is recomputed below where needed
+        boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0, OutTile{st.v, st.w, sou, i0, j0});
+        if (ACT && !DERIV) {  // interior cells of the sliver tile: record from the tile values
+            const int tid = threadIdx.x;
+            for (int idx = tid; idx < TY * TX; idx += NT) {
+                const int i = i0 + idx / TX, j = j0 + idx % TX;
+                if (i >= BAND && i < H - BAND && j >= BAND && j < W - BAND)
+                    record_activation(a, t, (int64_t)i * a.pitch + j,
+                                      st.u[(idx / TX + HALO_U) * SW + HALO_U + idx % TX], sou[idx]);
             }
         }
     }
-    if (!interior) boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0);
+}
+
+// Writes the output tile (new v, w in the stage, new u in sou) with TMA stores.
+__device__ __forceinline__ void store_tile(const StepMaps &tm, const Stage &st, const float *sou,
+                                           int i0, int j0) {
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tma_store_2d(&tm.ov, st.v, j0, i0);
+        tma_store_2d(&tm.ow, st.w, j0, i0);
+        tma_store_2d(&tm.ou, sou, j0, i0);
+        bulk_commit();
+    }
 }
 
 static_assert(sizeof(StepArgs) <= SMEM_ARGS_BYTES, "StepArgs does not fit its shared slot");
@@ -338,7 +485,8 @@ __global__ void __launch_bounds__(NT, 1) fk_step_kernel(const __grid_constant__ 
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     float *sux = reinterpret_cast<float *>(smem + 2 * SMEM_STAGE_BYTES);  // [SUX_H][TX]
     float *suy = sux + TX * SUX_H;                                          // [TY][SW]
-    uint64_t *bar = reinterpret_cast<uint64_t *>(suy + SW * TY);            // [2]
+    float *sou = suy + SW * TY;                                             // [TY][TX]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sou + TX * TY);            // [2]
     StepArgs *sa = reinterpret_cast<StepArgs *>(bar + 2);
 
     const int tid = threadIdx.x;
@@ -365,18 +513,23 @@ __global__ void __launch_bounds__(NT, 1) fk_step_kernel(const __grid_constant__ 
     for (int n = 0; tile < ntiles; ++n, tile += gridDim.x) {
         const int s = n & 1;
         const int next = tile + gridDim.x;
-        if (tid == 0 && next < ntiles)  // stage s^1 was released by the barrier ending tile n-1
-            issue_tile(tm, stage_at(smem, s ^ 1), &bar[s ^ 1], (next / ntx) * TY,
-                       (next % ntx) * TX);
+        if (tid == 0) {
+            bulk_wait_read();  // the stores of tile n-1 have read stage s^1 and sou
+            if (next < ntiles)
+                issue_tile(tm, stage_at(smem, s ^ 1), &bar[s ^ 1], (next / ntx) * TY,
+                           (next % ntx) * TX);
+        }
         const bool ok = mbar_wait_bounded(&bar[s], (n >> 1) & 1);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(a.status, kStatusTimeout);
             return;
         }
-        compute_tile<DERIV, ACT>(*sa, a.t, stage_at(smem, s), sux, suy, active, (tile / ntx) * TY,
-                                 (tile % ntx) * TX);
-        __syncthreads();  // stage s and the u_x/u_y buffers are free again
+        const int i0 = (tile / ntx) * TY, j0 = (tile % ntx) * TX;
+        process_tile<DERIV, ACT>(*sa, a.t, stage_at(smem, s), sux, suy, sou, active, i0, j0);
+        store_tile(tm, stage_at(smem, s), sou, i0, j0);
+        __syncthreads();  // the u_x/u_y buffers are free again
     }
+    if (tid == 0) bulk_wait_all();
 }
 
 // ---- batched kernel: persistent CTAs over the tiles of many tissues ------------------------
@@ -390,7 +543,8 @@ __global__ void __launch_bounds__(NT, 1)
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     float *sux = reinterpret_cast<float *>(smem + 2 * SMEM_STAGE_BYTES);
     float *suy = sux + TX * SUX_H;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(suy + SW * TY);
+    float *sou = suy + SW * TY;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sou + TX * TY);
     StepArgs *sa = reinterpret_cast<StepArgs *>(bar + 2);  // arguments of the current tile's tissue
 
     const int tid = threadIdx.x;
@@ -409,9 +563,13 @@ __global__ void __launch_bounds__(NT, 1)
     for (int n = 0; it < n_items; ++n, it += gridDim.x) {
         const int s = n & 1;
         const int next = it + gridDim.x;
-        if (tid == 0 && next < n_items) {
-            const BatchItem b = items[next];
-            issue_tile(maps[b.tissue].maps[parity], stage_at(smem, s ^ 1), &bar[s ^ 1], b.i0, b.j0);
+        if (tid == 0) {
+            bulk_wait_read();
+            if (next < n_items) {
+                const BatchItem b = items[next];
+                issue_tile(maps[b.tissue].maps[parity], stage_at(smem, s ^ 1), &bar[s ^ 1], b.i0,
+                           b.j0);
+            }
         }
         const BatchItem b = items[it];
         stage_args(sa, &tissues[b.tissue].args[parity]);  // this tissue's arguments
@@ -423,9 +581,11 @@ __global__ void __launch_bounds__(NT, 1)
         unsigned active = 0;
         for (int k = 0; k < sa->n_stim; ++k)
             if (stim_active(sa->stim[k], t)) active |= 1u << k;
-        compute_tile<false, ACT>(*sa, t, stage_at(smem, s), sux, suy, active, b.i0, b.j0);
+        process_tile<false, ACT>(*sa, t, stage_at(smem, s), sux, suy, sou, active, b.i0, b.j0);
+        store_tile(maps[b.tissue].maps[parity], stage_at(smem, s), sou, b.i0, b.j0);
         __syncthreads();
     }
+    if (tid == 0) bulk_wait_all();
 }
 
 __global__ void add_int_kernel(int *p, int v) { *p += v; }

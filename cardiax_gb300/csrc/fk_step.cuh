@@ -31,8 +31,9 @@ constexpr int SMEM_STAGE_BYTES = SMEM_U_BYTES + SMEM_D_BYTES + 2 * SMEM_VW_BYTES
 constexpr int SMEM_UX_BYTES = TX * SUX_H * 4;
 constexpr int SMEM_UY_BYTES = SW * TY * 4;
 constexpr int SMEM_ARGS_BYTES = 1024;  // staged StepArgs (static_assert in fk_step.cu)
-constexpr int SMEM_STEP_BYTES = 2 * SMEM_STAGE_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES + 16 +
-                                SMEM_ARGS_BYTES + 128;  // + 2 mbarriers + args + align
+constexpr int SMEM_OUT_BYTES = TX * TY * 4;  // the new u tile (new v, w overwrite the stage)
+constexpr int SMEM_STEP_BYTES = 2 * SMEM_STAGE_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES +
+                                SMEM_OUT_BYTES + 16 + SMEM_ARGS_BYTES + 128;
 // Cells within this distance of an edge take the per-cell boundary path (one-sided stencils
 // and edge padding reach 4 cells in).
 constexpr int BAND = 4;
@@ -56,9 +57,9 @@ struct StepArgs {
 enum : int { kStatusTimeout = 1 };
 
 // TMA descriptors of one step: u (box SW x SU_H), v and w (box TX x TY) of the input state,
-// and D (box SW x SD_H).
+// D (box SW x SD_H), and the three planes of the output state (box TX x TY, for the stores).
 struct StepMaps {
-    CUtensorMap u, v, w, d;
+    CUtensorMap u, v, w, d, ov, ow, ou;
 };
 
 // Launches one step (Euler update, or the derivative when `deriv`).  With a.act_last set, the

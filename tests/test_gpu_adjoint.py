@@ -1,0 +1,126 @@
+"""The hand-written adjoint (through torch.autograd) against float64 autodiff of the oracle
+(the stand-in for jax.grad of the reference) and central finite differences.
+
+Regime: smooth sub-threshold states (no gate flips between float32 and float64 trajectories),
+a sub-threshold stimulus so that the stimulated-cell masking is exercised.  Bar: relative error
+(norm-wise per gradient) <= 1e-3.
+"""
+import numpy as np
+import pytest
+import torch
+
+import fk_torch as FT
+
+pytestmark = pytest.mark.gpu
+
+P3 = (3.33, 19.6, 1250, 870, 41, 0.25, 12.5, 33.33, 29, 10, 0.85, 0.13, 0.04, 1)
+TOL = 1e-3
+
+
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _smooth(rng, shape, lo, hi):
+    H, W = shape
+    i, j = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    f = np.zeros(shape)
+    for _ in range(3):
+        ci, cj, s = rng.uniform(0, H), rng.uniform(0, W), rng.uniform(0.2, 0.5) * max(H, W)
+        f += rng.uniform(-1, 1) * np.exp(-((i - ci) ** 2 + (j - cj) ** 2) / (2 * s * s))
+    f = (f - f.min()) / (f.max() - f.min() + 1e-12)
+    return lo + (hi - lo) * f
+
+
+def _case(shape, seed):
+    rng = np.random.default_rng(seed)
+    H, W = shape
+    v0 = _smooth(rng, shape, 0.8, 1.0)
+    w0 = _smooth(rng, shape, 0.8, 1.0)
+    u0 = _smooth(rng, shape, 0.0, 0.09)
+    D = _smooth(rng, shape, 3e-4, 1e-3)
+    f = np.zeros(shape)
+    f[H // 3: H // 3 + 4, 2:7] = 0.5
+    stim = (3, 2, 1e9, f)
+    obs = [10, 30]
+    R = rng.standard_normal((len(obs), 3, H, W)) * np.array([0.1, 0.1, 1.0])[None, :, None, None]
+    return v0, w0, u0, D, stim, obs, R
+
+
+def _oracle_grads(v0, w0, u0, D, stim, obs, R):
+    t = lambda x: torch.tensor(x, dtype=torch.float64, requires_grad=True)  # noqa: E731
+    V, Wt, U, Dt = t(v0), t(w0), t(u0), t(D)
+    th = torch.tensor(P3[:13], dtype=torch.float64, requires_grad=True)
+    st = [(stim[0], stim[1], stim[2], torch.tensor(stim[3], dtype=torch.float64))]
+    state = (V, Wt, U)
+    L = 0
+    tcur = 0
+    for k, to in enumerate(obs):
+        state = FT.forward(state, tcur, to, th, 1.0, Dt, st, 0.01, 0.01)
+        tcur = to
+        L = L + sum((state[c] * torch.tensor(R[k, c])).sum() for c in range(3))
+    L.backward()
+    return V.grad.numpy(), Wt.grad.numpy(), U.grad.numpy(), Dt.grad.numpy(), th.grad.numpy()
+
+
+def _gpu_grads(v0, w0, u0, D, stim, obs, R, seg=None):
+    from cardiax_gb300.adjoint import rollout
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    dev = torch.device("cuda", 0)
+    g = lambda x: torch.tensor(x, dtype=torch.float32, device=dev, requires_grad=True)  # noqa: E731
+    V, Wt, U, Dt = g(v0), g(w0), g(u0), g(D)
+    th = torch.tensor(P3[:13], dtype=torch.float32, device=dev, requires_grad=True)
+    out = rollout(V, Wt, U, Dt, th, [Stimulus(Protocol(*stim[:3]), stim[3].astype(np.float32))],
+                  0, max(obs), obs, seg=seg)
+    L = (out * torch.tensor(R, dtype=torch.float32, device=dev)).sum()
+    L.backward()
+    return tuple(x.grad.detach().cpu().numpy() for x in (V, Wt, U, Dt, th))
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("shape,seg", [((20, 24), None), ((48, 40), 7), ((13, 70), 30)])
+def test_adjoint_matches_fp64_autodiff(shape, seg):
+    _gpu()
+    case = _case(shape, sum(shape))
+    ref = _oracle_grads(*case)
+    got = _gpu_grads(*case, seg=seg)
+    names = ("v0", "w0", "u0", "D", "theta")
+    for n, a, b in zip(names, got, ref):
+        e = _rel(a, b)
+        print(f"{shape} grad {n}: relative error {e:.2e}")
+        assert e <= TOL, (n, e)
+    # V_v enters only through a Heaviside gate
+    assert got[4][12] == 0.0
+
+
+def test_adjoint_matches_finite_differences_on_D():
+    """Central differences (eps = 1e-3 relative) of the float64 oracle on 8 seeded D entries."""
+    _gpu()
+    shape = (24, 28)
+    v0, w0, u0, D, stim, obs, R = _case(shape, 5)
+    got = _gpu_grads(v0, w0, u0, D, stim, obs, R)[3]
+    rng = np.random.default_rng(0)
+    st = [(stim[0], stim[1], stim[2], torch.tensor(stim[3], dtype=torch.float64))]
+    th = torch.tensor(P3[:13], dtype=torch.float64)
+
+    def loss(Dm):
+        state = tuple(torch.tensor(x, dtype=torch.float64) for x in (v0, w0, u0))
+        L, tcur = 0.0, 0
+        for k, to in enumerate(obs):
+            state = FT.forward(state, tcur, to, th, 1.0, torch.tensor(Dm), st, 0.01, 0.01)
+            tcur = to
+            L += float(sum((state[c] * torch.tensor(R[k, c])).sum() for c in range(3)))
+        return L
+
+    for _ in range(8):
+        i, j = int(rng.integers(0, shape[0])), int(rng.integers(0, shape[1]))
+        eps = 1e-3 * D[i, j]
+        Dp, Dm = D.copy(), D.copy()
+        Dp[i, j] += eps
+        Dm[i, j] -= eps
+        fd = (loss(Dp) - loss(Dm)) / (2 * eps)
+        assert abs(got[i, j] - fd) <= 1e-3 * max(abs(fd), 1e-3 * np.abs(got).max()), (i, j, got[i, j], fd)
