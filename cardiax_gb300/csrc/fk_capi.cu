@@ -234,6 +234,9 @@ const char *fk_status_string(int s) {
         case FK_ERR_CUDA: return "CUDA error";
         case FK_ERR_TENSORMAP: return "TMA descriptor encoding failed";
         case FK_ERR_DEVICE: return "device-side barrier timeout";
+        case FK_ERR_CAPACITY:
+            return "grid larger than the static scratch of fk_forward_euler_noalloc "
+                   "(H * pitch must be <= FK_NOALLOC_MAX_CELLS = 512 * 512)";
         default: return "unknown status";
     }
 }

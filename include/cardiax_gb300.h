@@ -40,7 +40,8 @@ typedef enum {
     FK_ERR_ARGUMENT = 5,   /* any other invalid argument (dx <= 0, t1 < t0, ...)   */
     FK_ERR_CUDA = 6,       /* a CUDA call failed                                   */
     FK_ERR_TENSORMAP = 7,  /* the TMA descriptor could not be encoded              */
-    FK_ERR_DEVICE = 8      /* a kernel reported a barrier timeout                  */
+    FK_ERR_DEVICE = 8,     /* a kernel reported a barrier timeout                  */
+    FK_ERR_CAPACITY = 9    /* grid larger than fk_forward_euler_noalloc's scratch  */
 } fk_status;
 
 /* The 14 Fenton-Karma parameters in the reference's field order (cardiax/params.py:4-18). */
@@ -92,6 +93,18 @@ int fk_euler_step(fk_grid g, const float *state, const float *D, const fk_params
 int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, const fk_params *p,
                      const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1,
                      double dt, double dx, void *stream);
+
+/* fk_forward_euler without the scratch argument, for callers that cannot allocate device memory
+ * (an XLA custom call, for instance, gets all of its buffers from XLA and must not allocate).
+ * No counterpart in the reference.  The scratch state is a file-scope device array of this
+ * library holding FK_NOALLOC_MAX_CELLS cells (H * pitch <= 512 * 512, 3 MiB per GPU for the
+ * life of the process); larger grids return FK_ERR_CAPACITY.  The first call on a device looks
+ * up the array's address (make it before any stream capture); calls that overlap on the GPU
+ * share the array and race; nothing needs clearing between calls. */
+#define FK_NOALLOC_MAX_CELLS (512 * 512)
+int fk_forward_euler_noalloc(fk_grid g, float *state, const float *D, const fk_params *p,
+                             const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1,
+                             double dt, double dx, void *stream);
 
 /* forward (cardiax/solve.py:168-222): for i in 0 .. n_checkpoints-2, advances from
  * checkpoints[i] to checkpoints[i+1] and writes that state to out + i * 3 * H * pitch.
