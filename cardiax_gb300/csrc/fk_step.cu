@@ -229,10 +229,10 @@ __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_rows, int
 // EDGE: the tile touches the grid edge (and is not a one-row or one-column sliver): the halo
 // is clamped and every derivative picks the reference's row type, exactly as the padded
 // arrays of cardiax/solve.py:29-32,49-54 do.
-template <bool DERIV, bool ACT, bool EDGE>
+template <bool DERIV, bool ACT, bool EDGE, class P1>
 __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const Stage &st,
                                              float *sux, float *suy, float *sou, unsigned active,
-                                             int i0, int j0) {
+                                             int i0, int j0, P1 &&after_pass1) {
     const int tid = threadIdx.x;
     const int H = a.H, W = a.W, pitch = a.pitch;
     const float rdx = a.rdx;
@@ -309,6 +309,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
         }
         suy[r * SW + c] = o * rdx;
     }
+    if (tid == 0) after_pass1();  // e.g. start the next tile's loads
     __syncthreads();
 
     // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
@@ -428,18 +429,18 @@ __device__ __forceinline__ bool is_sliver(int i0, int j0, int H, int W) {
 }
 
 // Interior tiles, clamped edge tiles, or slivers (interior passes + per-cell band).
-template <bool DERIV, bool ACT>
+template <bool DERIV, bool ACT, class P1>
 __device__ __forceinline__ void process_tile(const StepArgs &a, float t, const Stage &st,
                                              float *sux, float *suy, float *sou, unsigned active,
-                                             int i0, int j0) {
+                                             int i0, int j0, P1 &&after_pass1) {
     const int H = a.H, W = a.W;
     const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
     if (interior) {
-        compute_tile<DERIV, ACT, false>(a, t, st, sux, suy, sou, active, i0, j0);
+        compute_tile<DERIV, ACT, false>(a, t, st, sux, suy, sou, active, i0, j0, after_pass1);
     } else if (!is_sliver(i0, j0, H, W)) {
-        compute_tile<DERIV, ACT, true>(a, t, st, sux, suy, sou, active, i0, j0);
+        compute_tile<DERIV, ACT, true>(a, t, st, sux, suy, sou, active, i0, j0, after_pass1);
     } else {
-        compute_tile<DERIV, false, false>(a, t, st, sux, suy, sou, active, i0, j0);
+        compute_tile<DERIV, false, false>(a, t, st, sux, suy, sou, active, i0, j0, after_pass1);
         __syncthreads();  // every cell of this tile is recomputed below where needed
         boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0, OutTile{st.v, st.w, sou, i0, j0});
         if (ACT && !DERIV) {  // interior cells of the sliver tile: record from the tile values
@@ -513,21 +514,23 @@ __global__ void __launch_bounds__(NT, 1) fk_step_kernel(const __grid_constant__ 
     for (int n = 0; tile < ntiles; ++n, tile += gridDim.x) {
         const int s = n & 1;
         const int next = tile + gridDim.x;
-        if (tid == 0) {
-            bulk_wait_read();  // the stores of tile n-1 have read stage s^1 and sou
-            if (next < ntiles)
-                issue_tile(tm, stage_at(smem, s ^ 1), &bar[s ^ 1], (next / ntx) * TY,
-                           (next % ntx) * TX);
-        }
         const bool ok = mbar_wait_bounded(&bar[s], (n >> 1) & 1);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(a.status, kStatusTimeout);
             return;
         }
         const int i0 = (tile / ntx) * TY, j0 = (tile % ntx) * TX;
-        process_tile<DERIV, ACT>(*sa, a.t, stage_at(smem, s), sux, suy, sou, active, i0, j0);
-        store_tile(tm, stage_at(smem, s), sou, i0, j0);
-        __syncthreads();  // the u_x/u_y buffers are free again
+        // at the end of pass 1: the stores of tile n-1 have had a pass to read stage s^1 and
+        // sou; once they have, the loads of tile n+1 go into stage s^1
+        auto prefetch = [&] {
+            bulk_wait_read();
+            if (next < ntiles)
+                issue_tile(tm, stage_at(smem, s ^ 1), &bar[s ^ 1], (next / ntx) * TY,
+                           (next % ntx) * TX);
+        };
+        process_tile<DERIV, ACT>(*sa, a.t, stage_at(smem, s), sux, suy, sou, active, i0, j0,
+                                 prefetch);
+        store_tile(tm, stage_at(smem, s), sou, i0, j0);  // its barrier also frees sux, suy
     }
     if (tid == 0) bulk_wait_all();
 }
@@ -563,14 +566,6 @@ __global__ void __launch_bounds__(NT, 1)
     for (int n = 0; it < n_items; ++n, it += gridDim.x) {
         const int s = n & 1;
         const int next = it + gridDim.x;
-        if (tid == 0) {
-            bulk_wait_read();
-            if (next < n_items) {
-                const BatchItem b = items[next];
-                issue_tile(maps[b.tissue].maps[parity], stage_at(smem, s ^ 1), &bar[s ^ 1], b.i0,
-                           b.j0);
-            }
-        }
         const BatchItem b = items[it];
         stage_args(sa, &tissues[b.tissue].args[parity]);  // this tissue's arguments
         const bool ok = mbar_wait_bounded(&bar[s], (n >> 1) & 1);
@@ -581,9 +576,18 @@ __global__ void __launch_bounds__(NT, 1)
         unsigned active = 0;
         for (int k = 0; k < sa->n_stim; ++k)
             if (stim_active(sa->stim[k], t)) active |= 1u << k;
-        process_tile<false, ACT>(*sa, t, stage_at(smem, s), sux, suy, sou, active, b.i0, b.j0);
+        auto prefetch = [&] {
+            bulk_wait_read();
+            if (next < n_items) {
+                const BatchItem nb = items[next];
+                issue_tile(maps[nb.tissue].maps[parity], stage_at(smem, s ^ 1), &bar[s ^ 1], nb.i0,
+                           nb.j0);
+            }
+        };
+        process_tile<false, ACT>(*sa, t, stage_at(smem, s), sux, suy, sou, active, b.i0, b.j0,
+                                 prefetch);
         store_tile(maps[b.tissue].maps[parity], stage_at(smem, s), sou, b.i0, b.j0);
-        __syncthreads();
+        __syncthreads();  // the staged arguments are rewritten for the next item
     }
     if (tid == 0) bulk_wait_all();
 }
