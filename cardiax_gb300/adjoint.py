@@ -35,6 +35,19 @@ def _lib():
                                       ctypes.c_int, ctypes.c_int64, ctypes.c_double,
                                       ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.fk_recompute.restype = ctypes.c_int
+        L.fk_recompute.argtypes = [N.Grid, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                   ctypes.c_void_p, ctypes.POINTER(N.Params),
+                                   ctypes.POINTER(N.Stimulus), ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+        L.fk_adjoint_range.restype = ctypes.c_int
+        L.fk_adjoint_range.argtypes = [N.Grid, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                       ctypes.c_void_p, ctypes.POINTER(N.Params),
+                                       ctypes.POINTER(N.Stimulus), ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L._adjoint_bound = True
     return L
 
@@ -74,24 +87,22 @@ class Adjoint:
 
     # -- rollouts -----------------------------------------------------------------------------
     def rollout_gradient(self, state0: torch.Tensor, t0: int, t1: int, obs_times: Sequence[int],
-                         obs_grads: torch.Tensor, seg: int = None) -> torch.Tensor:
+                         obs_grads: torch.Tensor, seg: int = None, ckpts=None) -> torch.Tensor:
         """Backward pass of a rollout from ``state0`` ((3, H, pitch)) over steps t0 .. t1-1,
         where the loss depends on the states at ``obs_times`` (each in [t0, t1]) with
         dL/dx_{obs_times[k]} = obs_grads[k] ((n_obs, 3, H, pitch)).  Returns dL/dx_{t0};
         dL/dD and dL/dtheta accumulate in this object.  Uses checkpoints every ``seg`` steps
-        (default ceil(sqrt(T))) and recomputes one segment at a time."""
+        (default ceil(sqrt(T))) and recomputes one segment at a time; ``ckpts`` = the
+        [(step, state)] checkpoints at t0, t0+seg, ... when the caller kept them."""
         T = self.t
         n = t1 - t0
-        seg = seg or max(1, math.ceil(math.sqrt(max(n, 1))))
+        seg = seg or default_segment(n)
         obs_index = {}
         for k, tt in enumerate(obs_times):
             obs_index.setdefault(int(tt), []).append(k)
-        # forward: checkpoints at t0, t0+seg, ...
-        ckpts = []
-        T.state.copy_(state0)
-        for s in range(t0, t1, seg):
-            ckpts.append((s, T.state.clone()))
-            T.advance(s, min(s + seg, t1))
+        if ckpts is None:  # forward: checkpoints at t0, t0+seg, ...
+            ckpts = forward_checkpoints(T, state0, t0, t1, seg)
+        L = _lib()
         lam = torch.zeros_like(state0)
         lam_tmp = torch.empty_like(state0)
         if t1 in obs_index:
@@ -100,19 +111,48 @@ class Adjoint:
         buf = torch.empty((seg,) + tuple(state0.shape), dtype=state0.dtype, device=state0.device)
         for s, st in reversed(ckpts):
             e = min(s + seg, t1)
-            # recompute x_s .. x_{e-1} into buf
-            buf[0].copy_(st)
-            for k in range(1, e - s):
-                N.call("fk_euler_step", T.grid, buf[k - 1].data_ptr(), T.D.data_ptr(),
-                       ctypes.byref(T.params), T.stim, T.n_stim, s + k - 1, T.dt, T.dx,
-                       buf[k].data_ptr(), stream_handle())
-            for tt in range(e - 1, s - 1, -1):
-                self.step(buf[tt - s], tt, lam, lam_tmp)
-                lam, lam_tmp = lam_tmp, lam
-                if tt in obs_index:
-                    for k in obs_index[tt]:
-                        lam += obs_grads[k]
+            rc = L.fk_recompute(T.grid, st.data_ptr(), s, e - s, T.D.data_ptr(),
+                                ctypes.byref(T.params), T.stim, T.n_stim, T.dt, T.dx,
+                                buf.data_ptr(), stream_handle())
+            if rc:
+                raise N.FkError(rc, "fk_recompute")
+            inj = [(tt, k) for tt in range(s, e) for k in obs_index.get(tt, [])]
+            steps = (ctypes.c_int64 * max(1, len(inj)))(*[tt for tt, _ in inj])
+            grads = (ctypes.c_void_p * max(1, len(inj)))(*[obs_grads[k].data_ptr() for _, k in inj])
+            rc = L.fk_adjoint_range(T.grid, buf.data_ptr(), s, e - s, T.D.data_ptr(),
+                                    ctypes.byref(T.params), T.stim, T.n_stim, T.dt, T.dx,
+                                    lam.data_ptr(), lam_tmp.data_ptr(), steps, grads, len(inj),
+                                    self.gD.data_ptr(), self.gtheta.data_ptr(), stream_handle())
+            if rc:
+                raise N.FkError(rc, "fk_adjoint_range")
         return lam
+
+
+def default_segment(n_steps: int) -> int:
+    return max(1, math.ceil(math.sqrt(max(n_steps, 1))))
+
+
+def forward_checkpoints(T: Tissue, state0: torch.Tensor, t0: int, t1: int, seg: int,
+                        stops: Sequence[int] = ()):
+    """Advances ``T`` from ``state0`` over t0 .. t1-1 keeping the states at t0, t0+seg, ...;
+    also returns clones of the (v, w, u) planes at each step in ``stops``."""
+    ckpts, snaps = [], {}
+    T.state.copy_(state0)
+    marks = sorted(set(range(t0, t1, seg)) | {int(x) for x in stops if t0 <= int(x) <= t1})
+    cur = t0
+    for m in marks:
+        if m > cur:
+            T.advance(cur, m)
+            cur = m
+        if (m - t0) % seg == 0 and m < t1:
+            ckpts.append((m, T.state.clone()))
+        if m in stops:
+            snaps[m] = T.state[:, :, :T.W].clone()
+    if t1 > cur:
+        T.advance(cur, t1)
+        if t1 in stops:
+            snaps[t1] = T.state[:, :, :T.W].clone()
+    return (ckpts, snaps) if stops else ckpts
 
 
 class _Rollout(torch.autograd.Function):
@@ -125,22 +165,15 @@ class _Rollout(torch.autograd.Function):
         tis = Tissue((H, W), params, D.detach(), stimuli, dt=dt, dx=dx, device=u0.device)
         tis.set_state((v0.detach(), w0.detach(), u0.detach()))
         state0 = tis.state.clone()
-        obs = sorted(set(int(t) for t in obs_times))
+        t_end = max([t0] + [int(t) for t in obs_times])
+        seg = seg or default_segment(t_end - t0)
+        ckpts, snaps = forward_checkpoints(tis, state0, t0, t_end, seg, stops=list(obs_times))
         out = torch.empty((len(obs_times), 3, H, W), dtype=torch.float32, device=u0.device)
-        cur = t0
-        snaps = {}
-        if t0 in obs:
-            snaps[t0] = tis.state[:, :, :W].clone()
-        for t in obs:
-            if t <= cur:
-                continue
-            tis.advance(cur, t)
-            cur = t
-            snaps[t] = tis.state[:, :, :W].clone()
         for k, t in enumerate(obs_times):
             out[k] = snaps[int(t)]
         ctx.save_for_backward(state0)
-        ctx.tis, ctx.t0, ctx.t1, ctx.obs_times, ctx.seg, ctx.W = tis, t0, t1, list(obs_times), seg, W
+        ctx.tis, ctx.t0, ctx.t1, ctx.obs_times, ctx.seg, ctx.W = tis, t0, t_end, list(obs_times), seg, W
+        ctx.ckpts = ckpts
         return out
 
     @staticmethod
@@ -151,8 +184,9 @@ class _Rollout(torch.autograd.Function):
         g = torch.zeros((len(ctx.obs_times),) + tuple(state0.shape), dtype=torch.float32,
                         device=state0.device)
         g[..., :W] = grad_out.to(torch.float32)
-        t_end = max([ctx.t0] + [int(t) for t in ctx.obs_times])
-        lam0 = adj.rollout_gradient(state0, ctx.t0, t_end, ctx.obs_times, g, seg=ctx.seg)
+        lam0 = adj.rollout_gradient(state0, ctx.t0, ctx.t1, ctx.obs_times, g, seg=ctx.seg,
+                                    ckpts=ctx.ckpts)
+        ctx.ckpts = None
         gth = adj.grad_theta().to(torch.float32)
         return (lam0[0, :, :W], lam0[1, :, :W], lam0[2, :, :W], adj.grad_D().clone(), gth,
                 None, None, None, None, None, None, None, None)

@@ -147,8 +147,6 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
             StepMaps &sm = b->h_maps[k].maps[p];
             if (p) sm.d = b->h_maps[k].maps[0].d;
             if ((rc = make_plane_map(&sm.u, in + 2 * plane, t.g.H, t.g.W, t.g.pitch, SW, SU_H)) ||
-                (rc = make_plane_map(&sm.v, in, t.g.H, t.g.W, t.g.pitch, TX, TY)) ||
-                (rc = make_plane_map(&sm.w, in + plane, t.g.H, t.g.W, t.g.pitch, TX, TY)) ||
                 (rc = make_plane_map(&sm.ov, o, t.g.H, t.g.W, t.g.pitch, TX, TY)) ||
                 (rc = make_plane_map(&sm.ow, o + plane, t.g.H, t.g.W, t.g.pitch, TX, TY)) ||
                 (rc = make_plane_map(&sm.ou, o + 2 * plane, t.g.H, t.g.W, t.g.pitch, TX, TY)))

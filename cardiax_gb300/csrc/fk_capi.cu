@@ -163,8 +163,6 @@ struct MapCache {
         int ki, ko, rc;
         if ((rc = lookup(g, in, -1, &ki)) || (rc = lookup(g, out, ki, &ko))) return rc;
         sm.u = u[ki];
-        sm.v = v[ki];
-        sm.w = w[ki];
         sm.ov = v[ko];
         sm.ow = w[ko];
         sm.ou = ut[ko];
@@ -208,6 +206,12 @@ int step_once(const fk_grid &g, const float *in, float *out, const float *D, con
     }
     cudaError_t e = launch_step(sm, a, deriv, stream);
     return e == cudaSuccess ? FK_OK : FK_ERR_CUDA;
+}
+
+__global__ void add_state_kernel(float *dst, const float *src, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] += src[i];
 }
 
 __global__ void fill_state_kernel(float *s, int64_t plane) {
@@ -426,6 +430,64 @@ int fk_adjoint_step(fk_grid g, const float *state, const float *D, const fk_para
     a.n_stim = n_stimuli;
     a.m = make_model(*p);
     return launch_adjoint(a, (cudaStream_t)stream) == cudaSuccess ? FK_OK : FK_ERR_CUDA;
+}
+
+int fk_recompute(fk_grid g, const float *state, int64_t s, int64_t n, const float *D,
+                 const fk_params *p, const fk_stimulus *stimuli, int n_stimuli, double dt,
+                 double dx, float *buf, void *stream) {
+    int rc = common_checks(g, state, buf, D, p, dx);
+    if (rc) return rc;
+    if (n < 1 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
+    const Model m = make_model(*p);
+    const float rdx = 1.0f / (float)dx;
+    const int64_t ns = 3 * g.H * g.pitch;
+    cudaStream_t cs = (cudaStream_t)stream;
+    if (cudaMemcpyAsync(buf, state, sizeof(float) * ns, cudaMemcpyDeviceToDevice, cs) != cudaSuccess)
+        return FK_ERR_CUDA;
+    MapCache maps;
+    for (int64_t k = 1; k < n; ++k) {
+        rc = step_once(g, buf + (k - 1) * ns, buf + k * ns, D, m, st, n_stimuli, s + k - 1, (float)dt,
+                       rdx, false, tm_d, maps, status, cs);
+        if (rc) return rc;
+    }
+    return FK_OK;
+}
+
+int fk_adjoint_range(fk_grid g, const float *buf, int64_t s, int64_t n, const float *D,
+                     const fk_params *p, const fk_stimulus *stimuli, int n_stimuli, double dt,
+                     double dx, float *lam, float *lam_tmp, const int64_t *inj_steps,
+                     const float *const *inj_grads, int n_inj, float *grad_D,
+                     double *grad_theta_slots, void *stream) {
+    int rc = common_checks(g, buf, lam, D, p, dx);
+    if (rc) return rc;
+    if (!lam_tmp || (n_inj > 0 && (!inj_steps || !inj_grads))) return FK_ERR_NULL;
+    if (n < 1 || n_inj < 0 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    const int64_t ns = 3 * g.H * g.pitch;
+    cudaStream_t cs = (cudaStream_t)stream;
+    float *cur = lam, *other = lam_tmp;
+    for (int64_t k = n - 1; k >= 0; --k) {
+        rc = fk_adjoint_step(g, buf + k * ns, D, p, stimuli, n_stimuli, s + k, dt, dx, cur, other,
+                             grad_D, grad_theta_slots, stream);
+        if (rc) return rc;
+        float *tmp = cur;
+        cur = other;
+        other = tmp;
+        for (int j = 0; j < n_inj; ++j)
+            if (inj_steps[j] == s + k) {
+                add_state_kernel<<<1024, 256, 0, cs>>>(cur, inj_grads[j], ns);
+                if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;
+            }
+    }
+    if (cur != lam &&
+        cudaMemcpyAsync(lam, cur, sizeof(float) * ns, cudaMemcpyDeviceToDevice, cs) != cudaSuccess)
+        return FK_ERR_CUDA;
+    return FK_OK;
 }
 
 }  // extern "C"

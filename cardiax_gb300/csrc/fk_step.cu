@@ -175,9 +175,14 @@ __device__ __noinline__ void boundary_band(const StepArgs &a, float t, unsigned 
 __device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 __device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
 
-// Shared-memory buffers of one pipeline stage.
+// Shared-memory buffers of one pipeline stage (the haloed u and D tiles), and the tile's own
+// v, w values (registers, loaded at the start of the tile) and output tiles.
 struct Stage {
-    float *u, *d, *v, *w;
+    float *u, *d;
+};
+struct TileIO {
+    float4 v[RPT], w[RPT];   // input v, w of this thread's pass-2 cells
+    float *ov, *ow, *ou;     // dense output tiles
 };
 
 __device__ __forceinline__ Stage stage_at(unsigned char *base, int s) {
@@ -185,8 +190,6 @@ __device__ __forceinline__ Stage stage_at(unsigned char *base, int s) {
     Stage st;
     st.u = reinterpret_cast<float *>(p);
     st.d = reinterpret_cast<float *>(p + SMEM_U_BYTES);
-    st.v = reinterpret_cast<float *>(p + SMEM_U_BYTES + SMEM_D_BYTES);
-    st.w = st.v + TX * TY;
     return st;
 }
 
@@ -195,8 +198,22 @@ __device__ __forceinline__ void issue_tile(const StepMaps &tm, const Stage &st, 
     mbar_arrive_expect_tx(bar, SMEM_STAGE_BYTES);
     tma_load_2d(st.u, &tm.u, j0 - HALO_U, i0 - HALO_U, bar);
     tma_load_2d(st.d, &tm.d, j0 - HALO_U, i0 - HALO_D, bar);
-    tma_load_2d(st.v, &tm.v, j0, i0, bar);
-    tma_load_2d(st.w, &tm.w, j0, i0, bar);
+}
+
+// This thread's v, w for pass 2 (16-byte loads, zero outside the grid).
+__device__ __forceinline__ void load_vw(const StepArgs &a, int i0, int j0, TileIO &io) {
+    const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
+    const int j = j0 + 4 * tx;
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+        const int i = i0 + RPT * ty + k;
+        io.v[k] = io.w[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < a.H && j < a.W) {
+            const int64_t off = (int64_t)i * a.pitch + j;
+            io.v[k] = __ldg(reinterpret_cast<const float4 *>(a.v + off));
+            io.w[k] = __ldg(reinterpret_cast<const float4 *>(a.w + off));
+        }
+    }
 }
 
 // Edge tiles: replace the zero fill of out-of-grid halo cells by the reference's edge padding
@@ -231,8 +248,8 @@ __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_rows, int
 // arrays of cardiax/solve.py:29-32,49-54 do.
 template <bool DERIV, bool ACT, bool EDGE, class P1>
 __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const Stage &st,
-                                             float *sux, float *suy, float *sou, unsigned active,
-                                             int i0, int j0, P1 &&after_pass1) {
+                                             float *sux, float *suy, const TileIO &io,
+                                             unsigned active, int i0, int j0, P1 &&after_pass1) {
     const int tid = threadIdx.x;
     const int H = a.H, W = a.W, pitch = a.pitch;
     const float rdx = a.rdx;
@@ -315,7 +332,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
     // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
     const int tx = tid % NTX, ty = tid / NTX;
     const int j = j0 + 4 * tx;
-#pragma unroll 1
+#pragma unroll
     for (int k = 0; k < RPT; ++k) {
         const int r = RPT * ty + k;
         const int i = i0 + r;
@@ -349,7 +366,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
         const float4 y0 = ld4(yb), y1 = ld4(yb + 4), y2 = ld4(yb + 8);
         const float4 dl = ld4(db - 4), dr = ld4(db + 4);
         const float4 uc = ld4(su + (r + HALO_U) * SW + HALO_U + 4 * tx);
-        const float4 vc = ld4(st.v + r * TX + 4 * tx), wc = ld4(st.w + r * TX + 4 * tx);
+        const float4 vc = io.v[k], wc = io.w[k];
 
         const float f[12] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w,
                              y2.x, y2.y, y2.z, y2.w};
@@ -410,10 +427,9 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
                 ou[m] = fmaf(du, a.dt, uu[m]);
             }
         }
-        // new v, w overwrite this thread's own cells of the stage; new u goes to sou
-        st4(st.v + r * TX + 4 * tx, make_float4(ov[0], ov[1], ov[2], ov[3]));
-        st4(st.w + r * TX + 4 * tx, make_float4(ow[0], ow[1], ow[2], ow[3]));
-        st4(sou + r * TX + 4 * tx, make_float4(ou[0], ou[1], ou[2], ou[3]));
+        st4(io.ov + r * TX + 4 * tx, make_float4(ov[0], ov[1], ov[2], ov[3]));
+        st4(io.ow + r * TX + 4 * tx, make_float4(ow[0], ow[1], ow[2], ow[3]));
+        st4(io.ou + r * TX + 4 * tx, make_float4(ou[0], ou[1], ou[2], ou[3]));
         if (ACT && !DERIV && i < H) {
 #pragma unroll
             for (int m = 0; m < 4; ++m)
@@ -431,39 +447,40 @@ __device__ __forceinline__ bool is_sliver(int i0, int j0, int H, int W) {
 // Interior tiles, clamped edge tiles, or slivers (interior passes + per-cell band).
 template <bool DERIV, bool ACT, class P1>
 __device__ __forceinline__ void process_tile(const StepArgs &a, float t, const Stage &st,
-                                             float *sux, float *suy, float *sou, unsigned active,
-                                             int i0, int j0, P1 &&after_pass1) {
+                                             float *sux, float *suy, const TileIO &io,
+                                             unsigned active, int i0, int j0, P1 &&after_pass1) {
     const int H = a.H, W = a.W;
     const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
     if (interior) {
-        compute_tile<DERIV, ACT, false>(a, t, st, sux, suy, sou, active, i0, j0, after_pass1);
+        compute_tile<DERIV, ACT, false>(a, t, st, sux, suy, io, active, i0, j0, after_pass1);
     } else if (!is_sliver(i0, j0, H, W)) {
-        compute_tile<DERIV, ACT, true>(a, t, st, sux, suy, sou, active, i0, j0, after_pass1);
+        compute_tile<DERIV, ACT, true>(a, t, st, sux, suy, io, active, i0, j0, after_pass1);
     } else {
-        compute_tile<DERIV, false, false>(a, t, st, sux, suy, sou, active, i0, j0, after_pass1);
+        compute_tile<DERIV, false, false>(a, t, st, sux, suy, io, active, i0, j0, after_pass1);
         __syncthreads();  // every cell of this tile is recomputed below where needed
-        boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0, OutTile{st.v, st.w, sou, i0, j0});
+        boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0,
+                                     OutTile{io.ov, io.ow, io.ou, i0, j0});
         if (ACT && !DERIV) {  // interior cells of the sliver tile: record from the tile values
             const int tid = threadIdx.x;
             for (int idx = tid; idx < TY * TX; idx += NT) {
                 const int i = i0 + idx / TX, j = j0 + idx % TX;
                 if (i >= BAND && i < H - BAND && j >= BAND && j < W - BAND)
                     record_activation(a, t, (int64_t)i * a.pitch + j,
-                                      st.u[(idx / TX + HALO_U) * SW + HALO_U + idx % TX], sou[idx]);
+                                      st.u[(idx / TX + HALO_U) * SW + HALO_U + idx % TX],
+                                      io.ou[idx]);
             }
         }
     }
 }
 
-// Writes the output tile (new v, w in the stage, new u in sou) with TMA stores.
-__device__ __forceinline__ void store_tile(const StepMaps &tm, const Stage &st, const float *sou,
-                                           int i0, int j0) {
+// Writes the output tiles with TMA stores (after all threads have written them).
+__device__ __forceinline__ void store_tile(const StepMaps &tm, const TileIO &io, int i0, int j0) {
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
-        tma_store_2d(&tm.ov, st.v, j0, i0);
-        tma_store_2d(&tm.ow, st.w, j0, i0);
-        tma_store_2d(&tm.ou, sou, j0, i0);
+        tma_store_2d(&tm.ov, io.ov, j0, i0);
+        tma_store_2d(&tm.ow, io.ow, j0, i0);
+        tma_store_2d(&tm.ou, io.ou, j0, i0);
         bulk_commit();
     }
 }
@@ -482,55 +499,61 @@ template <bool DERIV, bool ACT>
 __global__ void __launch_bounds__(NT, 1) fk_step_kernel(const __grid_constant__ StepMaps tm,
                                                         const __grid_constant__ StepArgs a) {
     extern __shared__ unsigned char smem_raw[];
-    unsigned char *smem = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float *sux = reinterpret_cast<float *>(smem + 2 * SMEM_STAGE_BYTES);  // [SUX_H][TX]
-    float *suy = sux + TX * SUX_H;                                          // [TY][SW]
-    float *sou = suy + SW * TY;                                             // [TY][TX]
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sou + TX * TY);            // [2]
-    StepArgs *sa = reinterpret_cast<StepArgs *>(bar + 2);
+    // 128-byte aligned base, offset as a pointer so that the compiler keeps the shared-memory
+    // state space (integer address arithmetic would turn every access into a generic one)
+    unsigned char *smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
+    float *sux = reinterpret_cast<float *>(smem + NSTAGE * SMEM_STAGE_BYTES);  // [SUX_H][TX]
+    float *suy = sux + TX * SUX_H;                                               // [TY][SW]
+    TileIO io;
+    io.ov = suy + SW * TY;                                                       // [TY][TX] x 3
+    io.ow = io.ov + TX * TY;
+    io.ou = io.ow + TX * TY;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(io.ou + TX * TY);              // [NSTAGE]
+    StepArgs *sa = reinterpret_cast<StepArgs *>(bar + NSTAGE);
 
     const int tid = threadIdx.x;
     const int ntx = (a.W + TX - 1) / TX, nty = (a.H + TY - 1) / TY, ntiles = ntx * nty;
     stage_args(sa, &a);
     if (tid == 0) {
         prefetch_tensormap(&tm.u);
-        prefetch_tensormap(&tm.v);
-        prefetch_tensormap(&tm.w);
         prefetch_tensormap(&tm.d);
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int k = 0; k < NSTAGE; ++k) mbar_init(&bar[k], 1);
         fence_barrier_init();
     }
     __syncthreads();
+    auto tile_i0 = [&](int tl) { return (tl / ntx) * TY; };
+    auto tile_j0 = [&](int tl) { return (tl % ntx) * TX; };
     int tile = blockIdx.x;
-    if (tid == 0 && tile < ntiles)
-        issue_tile(tm, stage_at(smem, 0), &bar[0], (tile / ntx) * TY, (tile % ntx) * TX);
+    if (tid == 0)  // prologue: the first two tiles of this CTA
+        for (int k = 0; k < NSTAGE - 1; ++k) {
+            const int tl = tile + k * gridDim.x;
+            if (tl < ntiles) issue_tile(tm, stage_at(smem, k), &bar[k], tile_i0(tl), tile_j0(tl));
+        }
 
     unsigned active = 0;
     for (int s = 0; s < a.n_stim; ++s)
         if (stim_active(a.stim[s], a.t)) active |= 1u << s;
 
     for (int n = 0; tile < ntiles; ++n, tile += gridDim.x) {
-        const int s = n & 1;
-        const int next = tile + gridDim.x;
-        const bool ok = mbar_wait_bounded(&bar[s], (n >> 1) & 1);
+        const int s = n % NSTAGE;
+        const int i0 = tile_i0(tile), j0 = tile_j0(tile);
+        // tile n+2 goes into the stage of tile n-1, which every thread has finished reading
+        const int ahead = tile + (NSTAGE - 1) * gridDim.x;
+        if (tid == 0 && ahead < ntiles) {
+            const int sa2 = (n + NSTAGE - 1) % NSTAGE;
+            issue_tile(tm, stage_at(smem, sa2), &bar[sa2], tile_i0(ahead), tile_j0(ahead));
+        }
+        load_vw(*sa, i0, j0, io);
+        const bool ok = mbar_wait_bounded(&bar[s], (n / NSTAGE) & 1);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(a.status, kStatusTimeout);
             return;
         }
-        const int i0 = (tile / ntx) * TY, j0 = (tile % ntx) * TX;
-        // at the end of pass 1: the stores of tile n-1 have had a pass to read stage s^1 and
-        // sou; once they have, the loads of tile n+1 go into stage s^1
-        auto prefetch = [&] {
-            bulk_wait_read();
-            if (next < ntiles)
-                issue_tile(tm, stage_at(smem, s ^ 1), &bar[s ^ 1], (next / ntx) * TY,
-                           (next % ntx) * TX);
-        };
-        process_tile<DERIV, ACT>(*sa, a.t, stage_at(smem, s), sux, suy, sou, active, i0, j0,
-                                 prefetch);
-        store_tile(tm, stage_at(smem, s), sou, i0, j0);  // its barrier also frees sux, suy
+        // before pass 2 rewrites the output tiles, the stores of tile n-1 must have read them
+        auto outputs_free = [&] { bulk_wait_read(); };
+        process_tile<DERIV, ACT>(*sa, a.t, stage_at(smem, s), sux, suy, io, active, i0, j0,
+                                 outputs_free);
+        store_tile(tm, io, i0, j0);  // its barrier also frees sux, suy and stage s
     }
     if (tid == 0) bulk_wait_all();
 }
@@ -542,33 +565,45 @@ __global__ void __launch_bounds__(NT, 1)
                     const BatchItem *__restrict__ items, int n_items, const int *t_dev,
                     int t_offset, int parity, int *status) {
     extern __shared__ unsigned char smem_raw[];
-    unsigned char *smem = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float *sux = reinterpret_cast<float *>(smem + 2 * SMEM_STAGE_BYTES);
+    unsigned char *smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
+    float *sux = reinterpret_cast<float *>(smem + NSTAGE * SMEM_STAGE_BYTES);
     float *suy = sux + TX * SUX_H;
-    float *sou = suy + SW * TY;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sou + TX * TY);
-    StepArgs *sa = reinterpret_cast<StepArgs *>(bar + 2);  // arguments of the current tile's tissue
+    TileIO io;
+    io.ov = suy + SW * TY;
+    io.ow = io.ov + TX * TY;
+    io.ou = io.ow + TX * TY;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(io.ou + TX * TY);
+    StepArgs *sa = reinterpret_cast<StepArgs *>(bar + NSTAGE);  // the current tile's tissue
 
     const int tid = threadIdx.x;
     const float t = (float)(*t_dev + t_offset);
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int k = 0; k < NSTAGE; ++k) mbar_init(&bar[k], 1);
         fence_barrier_init();
     }
     __syncthreads();
     int it = blockIdx.x;
-    if (tid == 0 && it < n_items) {
-        const BatchItem b = items[it];
-        issue_tile(maps[b.tissue].maps[parity], stage_at(smem, 0), &bar[0], b.i0, b.j0);
-    }
+    if (tid == 0)
+        for (int k = 0; k < NSTAGE - 1; ++k) {
+            const int x = it + k * gridDim.x;
+            if (x < n_items) {
+                const BatchItem b = items[x];
+                issue_tile(maps[b.tissue].maps[parity], stage_at(smem, k), &bar[k], b.i0, b.j0);
+            }
+        }
     for (int n = 0; it < n_items; ++n, it += gridDim.x) {
-        const int s = n & 1;
-        const int next = it + gridDim.x;
+        const int s = n % NSTAGE;
+        const int ahead = it + (NSTAGE - 1) * gridDim.x;
+        if (tid == 0 && ahead < n_items) {
+            const BatchItem b = items[ahead];
+            const int sa2 = (n + NSTAGE - 1) % NSTAGE;
+            issue_tile(maps[b.tissue].maps[parity], stage_at(smem, sa2), &bar[sa2], b.i0, b.j0);
+        }
         const BatchItem b = items[it];
         stage_args(sa, &tissues[b.tissue].args[parity]);  // this tissue's arguments
-        const bool ok = mbar_wait_bounded(&bar[s], (n >> 1) & 1);
+        __syncthreads();
+        load_vw(*sa, b.i0, b.j0, io);
+        const bool ok = mbar_wait_bounded(&bar[s], (n / NSTAGE) & 1);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(status, kStatusTimeout);
             return;
@@ -576,17 +611,10 @@ __global__ void __launch_bounds__(NT, 1)
         unsigned active = 0;
         for (int k = 0; k < sa->n_stim; ++k)
             if (stim_active(sa->stim[k], t)) active |= 1u << k;
-        auto prefetch = [&] {
-            bulk_wait_read();
-            if (next < n_items) {
-                const BatchItem nb = items[next];
-                issue_tile(maps[nb.tissue].maps[parity], stage_at(smem, s ^ 1), &bar[s ^ 1], nb.i0,
-                           nb.j0);
-            }
-        };
-        process_tile<false, ACT>(*sa, t, stage_at(smem, s), sux, suy, sou, active, b.i0, b.j0,
-                                 prefetch);
-        store_tile(maps[b.tissue].maps[parity], stage_at(smem, s), sou, b.i0, b.j0);
+        auto outputs_free = [&] { bulk_wait_read(); };
+        process_tile<false, ACT>(*sa, t, stage_at(smem, s), sux, suy, io, active, b.i0, b.j0,
+                                 outputs_free);
+        store_tile(maps[b.tissue].maps[parity], io, b.i0, b.j0);
         __syncthreads();  // the staged arguments are rewritten for the next item
     }
     if (tid == 0) bulk_wait_all();

@@ -9,8 +9,10 @@
 namespace fk {
 
 // Tile geometry of the step kernel.  A persistent CTA of NT threads (one per SM) walks over
-// TY x TX tiles with a two-stage TMA pipeline: the loads of tile n+1 are in flight while
-// tile n is computed.
+// TY x TX tiles with a three-stage TMA ring for the haloed u and D tiles (the loads of tiles
+// n+1 and n+2 are in flight while tile n is computed); v and w are read straight into
+// registers at the start of each tile, and the new state goes out through TMA stores from
+// dedicated output tiles.
 //   pass 1: u_x on rows -2 .. TY+1 and u_y on columns -2 .. TX+1 go to shared memory;
 //   pass 2: thread (tx, ty) owns columns 4tx .. 4tx+3 of rows RPT*ty .. RPT*ty+RPT-1.
 constexpr int TX = 128;
@@ -18,6 +20,7 @@ constexpr int TY = 32;
 constexpr int NT = 512;
 constexpr int NTX = TX / 4;          // float4 columns
 constexpr int RPT = TY / (NT / NTX); // rows per thread in pass 2
+constexpr int NSTAGE = 3;
 constexpr int HALO_U = 4;  // u_xx composes two radius-2 derivatives
 constexpr int HALO_D = 2;  // D_x is one radius-2 derivative
 constexpr int SW = TX + 2 * HALO_U;   // row width of the u, D and u_y tiles (16-byte multiple)
@@ -26,14 +29,13 @@ constexpr int SD_H = TY + 2 * HALO_D;
 constexpr int SUX_H = TY + 4;         // u_x rows -2 .. TY+1
 constexpr int SMEM_U_BYTES = SW * SU_H * 4;
 constexpr int SMEM_D_BYTES = SW * SD_H * 4;
-constexpr int SMEM_VW_BYTES = TX * TY * 4;  // one of the v, w tiles (no halo)
-constexpr int SMEM_STAGE_BYTES = SMEM_U_BYTES + SMEM_D_BYTES + 2 * SMEM_VW_BYTES;
+constexpr int SMEM_STAGE_BYTES = SMEM_U_BYTES + SMEM_D_BYTES;
 constexpr int SMEM_UX_BYTES = TX * SUX_H * 4;
 constexpr int SMEM_UY_BYTES = SW * TY * 4;
+constexpr int SMEM_PLANE_BYTES = TX * TY * 4;     // one dense output plane
 constexpr int SMEM_ARGS_BYTES = 1024;  // staged StepArgs (static_assert in fk_step.cu)
-constexpr int SMEM_OUT_BYTES = TX * TY * 4;  // the new u tile (new v, w overwrite the stage)
-constexpr int SMEM_STEP_BYTES = 2 * SMEM_STAGE_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES +
-                                SMEM_OUT_BYTES + 16 + SMEM_ARGS_BYTES + 128;
+constexpr int SMEM_STEP_BYTES = NSTAGE * SMEM_STAGE_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES +
+                                3 * SMEM_PLANE_BYTES + 8 * NSTAGE + SMEM_ARGS_BYTES + 128;
 // Cells within this distance of an edge take the per-cell boundary path (one-sided stencils
 // and edge padding reach 4 cells in).
 constexpr int BAND = 4;
@@ -56,10 +58,10 @@ struct StepArgs {
 
 enum : int { kStatusTimeout = 1 };
 
-// TMA descriptors of one step: u (box SW x SU_H), v and w (box TX x TY) of the input state,
-// D (box SW x SD_H), and the three planes of the output state (box TX x TY, for the stores).
+// TMA descriptors of one step: u (box SW x SU_H) of the input state, D (box SW x SD_H), and
+// the three planes of the output state (box TX x TY, for the stores).
 struct StepMaps {
-    CUtensorMap u, v, w, d, ov, ow, ou;
+    CUtensorMap u, d, ov, ow, ou;
 };
 
 // Launches one step (Euler update, or the derivative when `deriv`).  With a.act_last set, the

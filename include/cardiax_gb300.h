@@ -186,6 +186,21 @@ int fk_adjoint_step(fk_grid g, const float *state, const float *D, const fk_para
                     const float *lam_next, float *lam, float *grad_D, double *grad_theta_slots,
                     void *stream);
 
+/* Segment helpers of a checkpointed reverse pass (one C call per segment instead of one per
+ * step).  fk_recompute writes x_s (a copy of `state`) and x_{s+1} .. x_{s+n-1} into `buf`
+ * (n consecutive states).  fk_adjoint_range walks k = n-1 .. 0: lam <- adjoint step at
+ * x_{s+k} (buf[k]), then adds inj_grads[j] to lam for every j with inj_steps[j] == s+k.  On
+ * entry lam is the cotangent of x_{s+n}; on return that of x_s.  lam_tmp is a second state
+ * buffer.  Gradients accumulate as in fk_adjoint_step. */
+int fk_recompute(fk_grid g, const float *state, int64_t s, int64_t n, const float *D,
+                 const fk_params *p, const fk_stimulus *stimuli, int n_stimuli, double dt,
+                 double dx, float *buf, void *stream);
+int fk_adjoint_range(fk_grid g, const float *buf, int64_t s, int64_t n, const float *D,
+                     const fk_params *p, const fk_stimulus *stimuli, int n_stimuli, double dt,
+                     double dx, float *lam, float *lam_tmp, const int64_t *inj_steps,
+                     const float *const *inj_grads, int n_inj, float *grad_D,
+                     double *grad_theta_slots, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
