@@ -7,6 +7,8 @@
 //   fk_forward_euler  cardiax/solve.py:92-100  _forward_euler
 //   fk_forward_euler_tracked  the same, with activation-time maps (no reference counterpart)
 //   fk_forward        cardiax/solve.py:168-222 forward (Euler integrator)
+//   fk_heun_step      cardiax/solve.py:73-85   step_heun
+//   fk_forward_heun   cardiax/solve.py:103-111 _forward_heun
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
@@ -214,6 +216,20 @@ __global__ void add_state_kernel(float *dst, const float *src, int64_t n) {
         dst[i] += src[i];
 }
 
+// x1 = x + dt d (the first Heun stage; the same fused multiply-add as the Euler kernels)
+__global__ void heun_stage1_kernel(float *x1, const float *x, const float *d, float dt, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        x1[i] = fmaf(d[i], dt, x[i]);
+}
+// out = x + (d1 + d2) h, h = dt / 2 (cardiax/solve.py:80-84)
+__global__ void heun_combine_kernel(float *out, const float *x, const float *d1, const float *d2,
+                                    float h, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = fmaf(d1[i] + d2[i], h, x[i]);
+}
+
 __global__ void fill_state_kernel(float *s, int64_t plane) {
     int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -346,6 +362,72 @@ int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, co
                      double dt, double dx, void *stream) {
     return fk_forward_euler_tracked(g, state, scratch, D, p, stimuli, n_stimuli, t0, t1, dt, dx,
                                     nullptr, stream);
+}
+
+// One Heun step from `in` to `out` with work = [d1, x1, d2].
+static int heun_once(const fk_grid &g, const float *in, float *out, float *work, const float *D,
+                     const Model &m, const Stim *st, int ns, int64_t t, float dt, float rdx,
+                     const CUtensorMap &tm_d, MapCache &maps, int *status, cudaStream_t s) {
+    const int64_t n = 3 * g.H * g.pitch;
+    float *d1 = work, *x1 = work + n, *d2 = work + 2 * n;
+    int rc = step_once(g, in, d1, D, m, st, ns, t, 0.0f, rdx, true, tm_d, maps, status, s);
+    if (rc) return rc;
+    heun_stage1_kernel<<<1024, 256, 0, s>>>(x1, in, d1, dt, n);
+    if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;
+    if ((rc = step_once(g, x1, d2, D, m, st, ns, t, 0.0f, rdx, true, tm_d, maps, status, s)))
+        return rc;
+    heun_combine_kernel<<<1024, 256, 0, s>>>(out, in, d1, d2, dt * 0.5f, n);
+    return cudaGetLastError() == cudaSuccess ? FK_OK : FK_ERR_CUDA;
+}
+
+int fk_heun_step(fk_grid g, const float *state, const float *D, const fk_params *p,
+                 const fk_stimulus *stimuli, int n_stimuli, int64_t t, double dt, double dx,
+                 float *state_out, float *work, void *stream) {
+    int rc = common_checks(g, state, state_out, D, p, dx);
+    if (rc) return rc;
+    if (!work) return FK_ERR_NULL;
+    if (!aligned16(work)) return FK_ERR_ALIGN;
+    if (!std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
+    MapCache maps;
+    return heun_once(g, state, state_out, work, D, make_model(*p), st, n_stimuli, t, (float)dt,
+                     1.0f / (float)dx, tm_d, maps, status, (cudaStream_t)stream);
+}
+
+int fk_forward_heun(fk_grid g, float *state, float *work, const float *D, const fk_params *p,
+                    const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1, double dt,
+                    double dx, void *stream) {
+    int rc = common_checks(g, state, work, D, p, dx);
+    if (rc) return rc;
+    if (t1 < t0 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
+    const Model m = make_model(*p);
+    const float rdx = 1.0f / (float)dx;
+    const int64_t n = 3 * g.H * g.pitch;
+    cudaStream_t s = (cudaStream_t)stream;
+    float *other = work + 3 * n;  // the 4th work buffer is the ping-pong state
+    float *bufs[2] = {state, other};
+    MapCache maps;
+    for (int64_t t = t0; t < t1; ++t) {
+        const int k = (int)((t - t0) & 1);
+        if ((rc = heun_once(g, bufs[k], bufs[k ^ 1], work, D, m, st, n_stimuli, t, (float)dt, rdx,
+                            tm_d, maps, status, s)))
+            return rc;
+    }
+    if (((t1 - t0) & 1) &&
+        cudaMemcpyAsync(state, other, sizeof(float) * n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return FK_ERR_CUDA;
+    return FK_OK;
 }
 
 int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,

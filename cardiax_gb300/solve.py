@@ -12,12 +12,14 @@ function                 reference                                 C ABI
 ``_forward_euler``       cardiax/solve.py:92-100                   ``fk_forward_euler``
 ``forward``              cardiax/solve.py:168-222                  ``fk_forward``
 ``forward_dimensional``  cardiax/solve.py:133-165                  ``fk_forward``
+``step_heun``            cardiax/solve.py:73-85                    ``fk_heun_step``
+``_forward_heun``        cardiax/solve.py:103-111                  ``fk_forward_heun``
 =======================  =======================================  ==========================
 
 Arrays may be NumPy arrays or torch tensors; results are float32 torch tensors on the current
 CUDA device (views of pitched device buffers).  Like the reference these functions are pure:
-inputs are never modified.  Only the Euler integrator is implemented; plotting is not part of
-this package.
+inputs are never modified.  The Euler and Heun integrators are implemented; Dormand-Prince and
+plotting are not part of this package.
 """
 from __future__ import annotations
 
@@ -86,16 +88,38 @@ def _forward_euler(state, t, t_end, params, diffusivity, stimuli, dt, dx) -> Sta
     return _states(tis, out)[0]
 
 
+def step_heun(state, t, params, diffusivity, stimuli, dt, dx) -> State:
+    """One Heun step, both stages at step t (cardiax/solve.py:73-85)."""
+    tis = _tissue(state, params, diffusivity, stimuli, dt, dx)
+    tis.advance_heun(int(_scalar(t)), int(_scalar(t)) + 1)
+    return State(*tis.view())
+
+
+def _forward_heun(state, t, t_end, params, diffusivity, stimuli, dt, dx) -> State:
+    """The state after Heun steps t .. t_end-1 (cardiax/solve.py:103-111)."""
+    tis = _tissue(state, params, diffusivity, stimuli, dt, dx)
+    tis.advance_heun(int(_scalar(t)), int(_scalar(t_end)))
+    return State(*tis.view())
+
+
 def forward(state, checkpoints, params, diffusivity, stimuli, dt, dx,
             integrator=TimeIntegrator.EULER, plot_while=False) -> List[State]:
     """States at ``checkpoints[1:]`` (the initial state is not included), advancing with the
-    absolute step index driving the stimuli (cardiax/solve.py:168-222)."""
+    absolute step index driving the stimuli (cardiax/solve.py:168-222).  Euler and Heun
+    integrators; Dormand-Prince is not implemented."""
     if plot_while:
         raise NotImplementedError("plotting is not part of cardiax_gb300")
-    if integrator not in (TimeIntegrator.EULER, "euler"):
-        raise NotImplementedError("only the Euler integrator is implemented")
     tis = _tissue(state, params, diffusivity, stimuli, dt, dx)
-    return _states(tis, tis.forward(list(checkpoints)))
+    if integrator in (TimeIntegrator.EULER, "euler"):
+        return _states(tis, tis.forward(list(checkpoints)))
+    if integrator in (TimeIntegrator.HEUN, "heun"):
+        ck = [int(_scalar(c)) for c in checkpoints]
+        out = []
+        for a, b in zip(ck[:-1], ck[1:]):
+            tis.advance_heun(a, b)
+            out.append(State(*(x.clone() for x in tis.view())))
+        return out
+    raise NotImplementedError("only the Euler and Heun integrators are implemented")
 
 
 def forward_dimensional(tissue_size, final_time, ms_step, params, diffusivity, stimuli, dt, dx,

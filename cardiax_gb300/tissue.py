@@ -180,6 +180,16 @@ class Tissue:
                self.n_stim, int(t0), int(t1), self.dt, self.dx, act, stream_handle())
         return self
 
+    def advance_heun(self, t0: int, t1: int) -> "Tissue":
+        """Heun steps t0 .. t1-1 in place (cardiax/solve.py:103-111)."""
+        if getattr(self, "_heun_work", None) is None:
+            self._heun_work = torch.empty((4,) + tuple(self.state.shape), dtype=torch.float32,
+                                          device=self.device)
+        N.call("fk_forward_heun", self.grid, self.state.data_ptr(), self._heun_work.data_ptr(),
+               self.D.data_ptr(), ctypes.byref(self.params), self.stim, self.n_stim, int(t0),
+               int(t1), self.dt, self.dx, stream_handle())
+        return self
+
     def forward(self, checkpoints, out: torch.Tensor = None) -> torch.Tensor:
         """States at checkpoints[1:] starting from the current state, as a
         (len-1, 3, H, pitch) tensor (cardiax/solve.py:168-222).  The current state is not

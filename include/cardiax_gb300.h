@@ -106,6 +106,18 @@ int fk_forward_euler_noalloc(fk_grid g, float *state, const float *D, const fk_p
                              const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1,
                              double dt, double dx, void *stream);
 
+/* step_heun (cardiax/solve.py:73-85): x1 = x + dt f(x, t); out = x + (f(x, t) + f(x1, t)) dt/2,
+ * both stages at step index t as in the reference.  `work` holds 3 state buffers. */
+int fk_heun_step(fk_grid g, const float *state, const float *D, const fk_params *p,
+                 const fk_stimulus *stimuli, int n_stimuli, int64_t t, double dt, double dx,
+                 float *state_out, float *work, void *stream);
+
+/* _forward_heun (cardiax/solve.py:103-111): Heun steps t0 .. t1-1 applied to `state` in place;
+ * `work` holds 4 state buffers. */
+int fk_forward_heun(fk_grid g, float *state, float *work, const float *D, const fk_params *p,
+                    const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1, double dt,
+                    double dx, void *stream);
+
 /* forward (cardiax/solve.py:168-222): for i in 0 .. n_checkpoints-2, advances from
  * checkpoints[i] to checkpoints[i+1] and writes that state to out + i * 3 * H * pitch.
  * `state0` is only read; `scratch` is one state buffer.  Checkpoints must be non-decreasing. */

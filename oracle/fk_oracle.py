@@ -10,6 +10,8 @@ round the same way):
 * ``cardiax/solve.py:26-65``   ``step``       -> :func:`derivative`
 * ``cardiax/solve.py:68-70``   ``step_euler`` -> :func:`euler_step`
 * ``cardiax/solve.py:92-100``  ``_forward_euler`` -> :func:`forward_euler`
+* ``cardiax/solve.py:73-85,103-111`` ``step_heun``/``_forward_heun`` -> :func:`heun_step`,
+  :func:`forward_heun`
 * ``cardiax/solve.py:168-222`` ``forward``    -> :func:`forward`
 * ``cardiax/solve.py:225-254`` ``gradient``   -> :func:`gradient`
 * ``cardiax/solve.py:257-271`` ``stimulate``  -> :func:`stimulate`
@@ -142,6 +144,25 @@ def euler_step(state: OState, t, params, diffusivity, stimuli, dt, dx) -> OState
     g = derivative(state, t, params, diffusivity, stimuli, dx)
     h = state.u.dtype.type(dt)
     return OState(*(x + dxdt * h for x, dxdt in zip(state, g)))
+
+
+def heun_step(state: OState, t, params, diffusivity, stimuli, dt, dx) -> OState:
+    """Heun's method with both stages at step index t (cardiax/solve.py:73-85):
+    x1 = x + dt f(x, t);  x' = x + (f(x, t) + f(x1, t)) (dt / 2)."""
+    f = state.u.dtype.type
+    d1 = derivative(state, t, params, diffusivity, stimuli, dx)
+    x1 = OState(*(x + d * f(dt) for x, d in zip(state, d1)))
+    d2 = derivative(x1, t, params, diffusivity, stimuli, dx)
+    h = f(dt) * f(0.5)
+    return OState(*(x + (a + b) * h for x, a, b in zip(state, d1, d2)))
+
+
+def forward_heun(state: OState, t0, t1, params, diffusivity, stimuli, dt, dx) -> OState:
+    """Heun steps t0 .. t1-1 (cardiax/solve.py:103-111)."""
+    f = state.u.dtype.type
+    for i in range(int(t0), int(t1)):
+        state = heun_step(state, f(i), params, diffusivity, stimuli, dt, dx)
+    return state
 
 
 def forward_euler(state: OState, t0, t1, params, diffusivity, stimuli, dt, dx) -> OState:

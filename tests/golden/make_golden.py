@@ -15,6 +15,7 @@ Fixtures (all float32 unless noted; "x64" = the same code with float64, JAX's x6
 * ``gradient.npz``         -- ``solve.gradient`` along both axes on small arrays
 * ``step.npz``             -- ``solve.step`` derivatives on small grids with stimuli
 * ``forward_small.npz``    -- ``solve._forward_euler`` 0 -> 200 on 32x40 (float32 and x64)
+* ``heun_small.npz``       -- ``solve._forward_heun`` on the same case (float32 and x64)
 * ``config0.npz``          -- ``solve.forward`` on the 128x128 plain configuration (planar
   stimulus on the left 5 columns, amplitude 1.0, Protocol(0, 200, 1e9), checkpoints every
   100 steps to 1000) and its excitable variant (amplitude 20, Protocol(0, 2, 1e9))
@@ -131,6 +132,18 @@ def main(root: str):
             fs[f"{name}_{tag}"] = arr
     fs.update({"D": D, "f1": f1, "f2": f2})
     np.savez_compressed(os.path.join(out, "forward_small.npz"), **fs)
+
+    # --- Heun integrator on the same small case (cardiax/solve.py:73-85,103-111) -------------
+    hs = {}
+    for R_, dt_ in ((R, np.float32), (R64, np.float64)):
+        stims = [R_.stimulus.Stimulus(R_.stimulus.Protocol(0, 2, 1e9), f1.astype(dt_)),
+                 R_.stimulus.Stimulus(R_.stimulus.Protocol(60, 3, 1e9), f2.astype(dt_))]
+        res = R_.solve._forward_heun(R_.solve.init(shp), 0.0, 200.0, P.PARAMSET_3,
+                                     D.astype(dt_), stims, 0.01, 0.01)
+        tag = "f32" if dt_ == np.float32 else "f64"
+        for name, arr in zip("vwu", res):
+            hs[f"{name}_{tag}"] = arr
+    np.savez_compressed(os.path.join(out, "heun_small.npz"), **hs)
 
     # --- configuration 0 (128x128, 1000 steps) and its excitable variant ---------------------
     shp = (128, 128)

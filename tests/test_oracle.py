@@ -98,3 +98,15 @@ def test_params_golden():
     assert list(Pm.Params._fields) == rec["fields"]
     for name, vals in rec["sets"].items():
         assert [float(x) for x in getattr(Pm, name)] == vals, name
+
+
+@pytest.mark.parametrize("tag,dtype", [("f32", np.float32), ("f64", np.float64)])
+def test_heun_golden(golden, tag, dtype):
+    """The oracle's Heun integrator against the reference's own _forward_heun."""
+    g = golden("forward_small.npz")
+    h = golden("heun_small.npz")
+    stims = [O.OStim(0, 2, 1e9, g["f1"].astype(dtype)), O.OStim(60, 3, 1e9, g["f2"].astype(dtype))]
+    res = O.forward_heun(O.init(g["D"].shape, dtype), 0, 200, P3, g["D"].astype(dtype), stims,
+                         0.01, 0.01)
+    for name, arr in zip("vwu", res):
+        np.testing.assert_array_equal(arr, h[f"{name}_{tag}"])
