@@ -118,7 +118,7 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
     }
     int n_sm = 0;
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, b->device);
-    b->grid = n_sm > 0 ? n_sm : 1;
+    b->grid = n_sm > 0 ? n_sm * CTAS_PER_SM : 1;
     char *ws = static_cast<char *>(workspace);
     b->d_maps = reinterpret_cast<BatchMaps *>(ws + L.maps);
     b->d_tissues = reinterpret_cast<BatchTissue *>(ws + L.tissues);

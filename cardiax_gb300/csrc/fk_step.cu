@@ -262,7 +262,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
     }
 
     // ---- pass 1: u_x (tile rows -2 .. TY+1) and u_y (tile columns -2 .. TX+1) -------------
-#pragma unroll 1
+#pragma unroll PASS1_UNROLL
     for (int it = tid; it < SUX_H * NTX; it += NT) {
         const int r = it / NTX, q = it % NTX;
         const float *b = su + (r + 2) * SW + HALO_U + 4 * q;  // u row of ux row r
@@ -288,7 +288,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
         }
         st4(sux + r * TX + 4 * q, mul4(o, rdx));
     }
-#pragma unroll 1
+#pragma unroll PASS1_UNROLL
     for (int it = tid; it < TY * NTX; it += NT) {
         const int r = it / NTX, q = it % NTX;
         const float *b = su + (r + HALO_U) * SW + 4 * q;  // columns j0+4q-4 .. j0+4q+7
@@ -496,7 +496,7 @@ __device__ __forceinline__ void stage_args(StepArgs *dst, const StepArgs *src) {
 
 // ---- the step kernel: persistent CTAs over the tiles of one tissue ------------------------
 template <bool DERIV, bool ACT>
-__global__ void __launch_bounds__(NT, 1) fk_step_kernel(const __grid_constant__ StepMaps tm,
+__global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_constant__ StepMaps tm,
                                                         const __grid_constant__ StepArgs a) {
     extern __shared__ unsigned char smem_raw[];
     // 128-byte aligned base, offset as a pointer so that the compiler keeps the shared-memory
@@ -560,7 +560,7 @@ __global__ void __launch_bounds__(NT, 1) fk_step_kernel(const __grid_constant__ 
 
 // ---- batched kernel: persistent CTAs over the tiles of many tissues ------------------------
 template <bool ACT>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(NT, CTAS_PER_SM)
     fk_batch_kernel(const BatchTissue *__restrict__ tissues, const BatchMaps *__restrict__ maps,
                     const BatchItem *__restrict__ items, int n_items, const int *t_dev,
                     int t_offset, int parity, int *status) {
@@ -697,7 +697,7 @@ cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cud
     if (n_sm == 0 && cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return cudaErrorInvalidValue;
     const int ntiles = ((a.W + TX - 1) / TX) * ((a.H + TY - 1) / TY);
-    const int grid = ntiles < n_sm ? ntiles : n_sm;
+    const int grid = ntiles < n_sm * CTAS_PER_SM ? ntiles : n_sm * CTAS_PER_SM;
     if (deriv)
         fk_step_kernel<true, false><<<grid, NT, SMEM_STEP_BYTES, stream>>>(maps, a);
     else if (a.act_last)

@@ -15,9 +15,23 @@ namespace fk {
 // dedicated output tiles.
 //   pass 1: u_x on rows -2 .. TY+1 and u_y on columns -2 .. TX+1 go to shared memory;
 //   pass 2: thread (tx, ty) owns columns 4tx .. 4tx+3 of rows RPT*ty .. RPT*ty+RPT-1.
-constexpr int TX = 128;
-constexpr int TY = 32;
-constexpr int NT = 512;
+#ifndef FK_TILE_X
+#define FK_TILE_X 128
+#endif
+#ifndef FK_TILE_Y
+#define FK_TILE_Y 32
+#endif
+#ifndef FK_THREADS
+#define FK_THREADS 512
+#endif
+#ifndef FK_PASS1_UNROLL
+#define FK_PASS1_UNROLL 1
+#endif
+constexpr int TX = FK_TILE_X;
+constexpr int TY = FK_TILE_Y;
+constexpr int NT = FK_THREADS;
+constexpr int CTAS_PER_SM = NT <= 256 ? 2 : 1;
+constexpr int PASS1_UNROLL = FK_PASS1_UNROLL;
 constexpr int NTX = TX / 4;          // float4 columns
 constexpr int RPT = TY / (NT / NTX); // rows per thread in pass 2
 constexpr int NSTAGE = 3;
