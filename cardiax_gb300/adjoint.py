@@ -202,3 +202,78 @@ def rollout(v0, w0, u0, D, theta, stimuli, t0: int, t1: int, obs_times: Sequence
     to = lambda x: x if isinstance(x, torch.Tensor) and x.is_cuda else as_cuda_f32(x, dev)  # noqa: E731
     return _Rollout.apply(to(v0), to(w0), to(u0), to(D), to(theta), Cm, list(stimuli), int(t0),
                           int(t1), list(obs_times), float(dt), float(dx), seg)
+
+
+class _RolloutBatch(torch.autograd.Function):
+    """States at ``obs_times`` of B tissues sharing D and theta (one stimulus list per tissue);
+    each tissue's forward and backward run on its own CUDA stream so the GPU overlaps them."""
+
+    @staticmethod
+    def forward(ctx, states0, D, theta, Cm, stimuli, t0, t1, obs_times, dt, dx, seg):
+        params = [float(x) for x in theta.detach().cpu().tolist()] + [float(Cm)]
+        B, _, H, W = states0.shape
+        dev = states0.device
+        t_end = max([t0] + [int(t) for t in obs_times])
+        seg = seg or default_segment(t_end - t0)
+        out = torch.empty((B, len(obs_times), 3, H, W), dtype=torch.float32, device=dev)
+        main = torch.cuda.current_stream(dev)
+        streams = [torch.cuda.Stream(dev) for _ in range(B)]
+        tissues, ckpts, state0s = [], [], []
+        for b in range(B):
+            streams[b].wait_stream(main)
+            with torch.cuda.stream(streams[b]):
+                tis = Tissue((H, W), params, D.detach(), stimuli[b], dt=dt, dx=dx, device=dev)
+                tis.set_state(states0[b].detach())
+                s0 = tis.state.clone()
+                ck, snaps = forward_checkpoints(tis, s0, t0, t_end, seg, stops=list(obs_times))
+                for k, t in enumerate(obs_times):
+                    out[b, k] = snaps[int(t)]
+            tissues.append(tis)
+            ckpts.append(ck)
+            state0s.append(s0)
+        for s in streams:
+            main.wait_stream(s)
+        ctx.tissues, ctx.ckpts, ctx.state0s, ctx.streams = tissues, ckpts, state0s, streams
+        ctx.t0, ctx.t1, ctx.obs_times, ctx.seg, ctx.W = t0, t_end, list(obs_times), seg, W
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        W = ctx.W
+        main = torch.cuda.current_stream()
+        B = len(ctx.tissues)
+        g0 = []
+        adjs = []
+        for b in range(B):
+            s = ctx.streams[b]
+            s.wait_stream(main)
+            with torch.cuda.stream(s):
+                tis = ctx.tissues[b]
+                adj = Adjoint(tis)
+                g = torch.zeros((len(ctx.obs_times),) + tuple(ctx.state0s[b].shape),
+                                dtype=torch.float32, device=tis.device)
+                g[..., :W] = grad_out[b].to(torch.float32)
+                lam0 = adj.rollout_gradient(ctx.state0s[b], ctx.t0, ctx.t1, ctx.obs_times, g,
+                                            seg=ctx.seg, ckpts=ctx.ckpts[b])
+                g0.append(lam0[:, :, :W])
+                adjs.append(adj)
+        for s in ctx.streams:
+            main.wait_stream(s)
+        ctx.ckpts = None
+        gD = adjs[0].grad_D().clone()
+        gth = adjs[0].grad_theta()
+        for a in adjs[1:]:  # fixed order: deterministic sums
+            gD += a.grad_D()
+            gth = gth + a.grad_theta()
+        return (torch.stack(g0), gD, gth.to(torch.float32), None, None, None, None, None, None,
+                None, None)
+
+
+def rollout_batch(states0, D, theta, stimuli_per_tissue, t0: int, t1: int,
+                  obs_times: Sequence[int], dt: float = 0.01, dx: float = 0.01, Cm: float = 1.0,
+                  seg: int = None):
+    """Differentiable rollouts of B tissues that share D and theta: ``states0`` is
+    (B, 3, H, W) (v, w, u), ``stimuli_per_tissue`` a list of B stimulus lists.  Returns
+    (B, n_obs, 3, H, W); gradients flow to states0, D (summed over tissues) and theta."""
+    return _RolloutBatch.apply(states0, D, theta, Cm, [list(s) for s in stimuli_per_tissue],
+                               int(t0), int(t1), list(obs_times), float(dt), float(dx), seg)

@@ -210,77 +210,76 @@ __global__ void __launch_bounds__(AB *AB)
         }
         // gth[12] (V_v) enters only through a Heaviside gate: zero
 
-        // ---- diffusion transpose and dL/dD ---------------------------------------------
+        // ---- diffusion transpose and dL/dD, axis by axis --------------------------------
+        // Along an axis, a cell at least ADJ_BAND from both ends uses the interior form
+        // (G^T = -G); otherwise the explicit transposed rows and the edge-pad fold.
         const float *D = a.D, *U = a.u, *LU = a.lu;
-        float diff_u, gD;
-        const bool interior = i >= ADJ_BAND && i < H - ADJ_BAND && j >= ADJ_BAND && j < W - ADJ_BAND;
-        if (interior) {
-            auto Dat = [&](int r, int c) { return __ldg(D + (int64_t)r * pitch + c); };
-            auto Uat = [&](int r, int c) { return __ldg(U + (int64_t)r * pitch + c); };
-            auto Mat = [&](int r, int c) { return dt * __ldg(LU + (int64_t)r * pitch + c); };
-            // first derivatives (scaled) at (r, c)
-            auto Dx = [&](int r, int c) {
-                return g_central(Dat(r - 2, c), Dat(r - 1, c), Dat(r + 1, c), Dat(r + 2, c)) * rdx;
+        auto Dat = [&](int r, int c) { return __ldg(D + (int64_t)r * pitch + c); };
+        auto Uat = [&](int r, int c) { return __ldg(U + (int64_t)r * pitch + c); };
+        auto Mat = [&](int r, int c) { return dt * __ldg(LU + (int64_t)r * pitch + c); };
+        float ATx, BTx, uxx, gx, ATy, BTy, uyy, gy;
+        if (i >= ADJ_BAND && i < H - ADJ_BAND) {
+            auto Dx = [&](int r) {
+                return g_central(Dat(r - 2, j), Dat(r - 1, j), Dat(r + 1, j), Dat(r + 2, j)) * rdx;
             };
-            auto Dy = [&](int r, int c) {
-                return g_central(Dat(r, c - 2), Dat(r, c - 1), Dat(r, c + 1), Dat(r, c + 2)) * rdx;
+            auto Ux = [&](int r) {
+                return g_central(Uat(r - 2, j), Uat(r - 1, j), Uat(r + 1, j), Uat(r + 2, j)) * rdx;
             };
-            auto Ux = [&](int r, int c) {
-                return g_central(Uat(r - 2, c), Uat(r - 1, c), Uat(r + 1, c), Uat(r + 2, c)) * rdx;
-            };
-            auto Uy = [&](int r, int c) {
-                return g_central(Uat(r, c - 2), Uat(r, c - 1), Uat(r, c + 1), Uat(r, c + 2)) * rdx;
-            };
-            // q = D mu; A^T q = G(G q) / dx^2 along each axis
-            auto Qx1 = [&](int r) {  // G_x(D mu) at (r, j) scaled
+            auto Q1 = [&](int r) {  // G_x(D mu) at (r, j), scaled
                 return g_central(Dat(r - 2, j) * Mat(r - 2, j), Dat(r - 1, j) * Mat(r - 1, j),
                                  Dat(r + 1, j) * Mat(r + 1, j), Dat(r + 2, j) * Mat(r + 2, j)) * rdx;
             };
-            auto Qy1 = [&](int c) {
+            ATx = g_central(Q1(i - 2), Q1(i - 1), Q1(i + 1), Q1(i + 2)) * rdx;
+            BTx = -g_central(Dx(i - 2) * Mat(i - 2, j), Dx(i - 1) * Mat(i - 1, j),
+                             Dx(i + 1) * Mat(i + 1, j), Dx(i + 2) * Mat(i + 2, j)) * rdx;
+            const float ux_m2 = Ux(i - 2), ux_m1 = Ux(i - 1), ux_p1 = Ux(i + 1), ux_p2 = Ux(i + 2);
+            uxx = g_central(ux_m2, ux_m1, ux_p1, ux_p2) * rdx;
+            gx = -g_central(Mat(i - 2, j) * ux_m2, Mat(i - 1, j) * ux_m1, Mat(i + 1, j) * ux_p1,
+                            Mat(i + 2, j) * ux_p2) * rdx;
+        } else {
+            auto Dx_at = [&](int r) { return fwd_d1([&](int x) { return at(D, x, j); }, r, H) * rdx; };
+            auto Ux_at = [&](int r) { return fwd_d1([&](int x) { return at(U, x, j); }, r, H) * rdx; };
+            auto Mcol = [&](int r) { return dt * __ldg(LU + (int64_t)r * pitch + j); };
+            const auto qx = make_line([&](int r) { return at(D, r, j) * Mcol(r); }, H);
+            const auto bx = make_line([&](int r) { return Dx_at(r) * Mcol(r); }, H);
+            const auto gxl = make_line([&](int r) { return Mcol(r) * Ux_at(r); }, H);
+            ATx = qx.AT(i) * (rdx * rdx);
+            BTx = bx.BT(i) * rdx;
+            uxx = fwd_d2([&](int r) { return at(U, r, j); }, i, H, rdx);
+            gx = gxl.BT(i) * rdx;
+        }
+        if (j >= ADJ_BAND && j < W - ADJ_BAND) {
+            auto Dy = [&](int c) {
+                return g_central(Dat(i, c - 2), Dat(i, c - 1), Dat(i, c + 1), Dat(i, c + 2)) * rdx;
+            };
+            auto Uy = [&](int c) {
+                return g_central(Uat(i, c - 2), Uat(i, c - 1), Uat(i, c + 1), Uat(i, c + 2)) * rdx;
+            };
+            auto Q1 = [&](int c) {
                 return g_central(Dat(i, c - 2) * Mat(i, c - 2), Dat(i, c - 1) * Mat(i, c - 1),
                                  Dat(i, c + 1) * Mat(i, c + 1), Dat(i, c + 2) * Mat(i, c + 2)) * rdx;
             };
-            const float ATx = g_central(Qx1(i - 2), Qx1(i - 1), Qx1(i + 1), Qx1(i + 2)) * rdx;
-            const float ATy = g_central(Qy1(j - 2), Qy1(j - 1), Qy1(j + 1), Qy1(j + 2)) * rdx;
-            // B^T ((B D) mu) = -G((B D) mu) / dx
-            const float BTx = -g_central(Dx(i - 2, j) * Mat(i - 2, j), Dx(i - 1, j) * Mat(i - 1, j),
-                                         Dx(i + 1, j) * Mat(i + 1, j), Dx(i + 2, j) * Mat(i + 2, j)) * rdx;
-            const float BTy = -g_central(Dy(i, j - 2) * Mat(i, j - 2), Dy(i, j - 1) * Mat(i, j - 1),
-                                         Dy(i, j + 1) * Mat(i, j + 1), Dy(i, j + 2) * Mat(i, j + 2)) * rdx;
-            diff_u = (ATx + ATy) + (BTx + BTy);
-            // dL/dD: mu (u_xx + u_yy) + B^T(mu u_x) + B^T(mu u_y)
-            const float uxx = g_central(Ux(i - 2, j), Ux(i - 1, j), Ux(i + 1, j), Ux(i + 2, j)) * rdx;
-            const float uyy = g_central(Uy(i, j - 2), Uy(i, j - 1), Uy(i, j + 1), Uy(i, j + 2)) * rdx;
-            const float gx = -g_central(Mat(i - 2, j) * Ux(i - 2, j), Mat(i - 1, j) * Ux(i - 1, j),
-                                        Mat(i + 1, j) * Ux(i + 1, j), Mat(i + 2, j) * Ux(i + 2, j)) * rdx;
-            const float gy = -g_central(Mat(i, j - 2) * Uy(i, j - 2), Mat(i, j - 1) * Uy(i, j - 1),
-                                        Mat(i, j + 1) * Uy(i, j + 1), Mat(i, j + 2) * Uy(i, j + 2)) * rdx;
-            gD = mu * (uxx + uyy) + (gx + gy);
+            ATy = g_central(Q1(j - 2), Q1(j - 1), Q1(j + 1), Q1(j + 2)) * rdx;
+            BTy = -g_central(Dy(j - 2) * Mat(i, j - 2), Dy(j - 1) * Mat(i, j - 1),
+                             Dy(j + 1) * Mat(i, j + 1), Dy(j + 2) * Mat(i, j + 2)) * rdx;
+            const float uy_m2 = Uy(j - 2), uy_m1 = Uy(j - 1), uy_p1 = Uy(j + 1), uy_p2 = Uy(j + 2);
+            uyy = g_central(uy_m2, uy_m1, uy_p1, uy_p2) * rdx;
+            gy = -g_central(Mat(i, j - 2) * uy_m2, Mat(i, j - 1) * uy_m1, Mat(i, j + 1) * uy_p1,
+                            Mat(i, j + 2) * uy_p2) * rdx;
         } else {
-            // generic: explicit transposed rows with the edge pad
-            auto colD = [&](int r) { return at(D, r, j); };
-            auto rowD = [&](int c) { return at(D, i, c); };
-            auto colU = [&](int r) { return at(U, r, j); };
-            auto rowU = [&](int c) { return at(U, i, c); };
-            auto Dx_at = [&](int r) {  // (B_x D)(r, j), r interior
-                return fwd_d1([&](int x) { return at(D, x, j); }, r, H) * rdx;
-            };
             auto Dy_at = [&](int c) { return fwd_d1([&](int y) { return at(D, i, y); }, c, W) * rdx; };
-            auto Ux_at = [&](int r) { return fwd_d1([&](int x) { return at(U, x, j); }, r, H) * rdx; };
             auto Uy_at = [&](int c) { return fwd_d1([&](int y) { return at(U, i, y); }, c, W) * rdx; };
-            auto Mcol = [&](int r) { return dt * __ldg(LU + (int64_t)r * pitch + j); };
             auto Mrow = [&](int c) { return dt * __ldg(LU + (int64_t)i * pitch + c); };
-            const auto qx = make_line([&](int r) { return colD(r) * Mcol(r); }, H);
-            const auto qy = make_line([&](int c) { return rowD(c) * Mrow(c); }, W);
-            const auto bx = make_line([&](int r) { return Dx_at(r) * Mcol(r); }, H);
+            const auto qy = make_line([&](int c) { return at(D, i, c) * Mrow(c); }, W);
             const auto by = make_line([&](int c) { return Dy_at(c) * Mrow(c); }, W);
-            diff_u = (qx.AT(i) * (rdx * rdx) + qy.AT(j) * (rdx * rdx)) +
-                     (bx.BT(i) * rdx + by.BT(j) * rdx);
-            const float uxx = fwd_d2(colU, i, H, rdx), uyy = fwd_d2(rowU, j, W, rdx);
-            const auto gxl = make_line([&](int r) { return Mcol(r) * Ux_at(r); }, H);
             const auto gyl = make_line([&](int c) { return Mrow(c) * Uy_at(c); }, W);
-            gD = mu * (uxx + uyy) + (gxl.BT(i) * rdx + gyl.BT(j) * rdx);
+            ATy = qy.AT(j) * (rdx * rdx);
+            BTy = by.BT(j) * rdx;
+            uyy = fwd_d2([&](int c) { return at(U, i, c); }, j, W, rdx);
+            gy = gyl.BT(j) * rdx;
         }
+        const float diff_u = (ATx + ATy) + (BTx + BTy);
+        const float gD = mu * (uxx + uyy) + (gx + gy);
         olu += diff_u;
         a.olv[off] = olv;
         a.olw[off] = olw;

@@ -124,3 +124,32 @@ def test_adjoint_matches_finite_differences_on_D():
         Dm[i, j] -= eps
         fd = (loss(Dp) - loss(Dm)) / (2 * eps)
         assert abs(got[i, j] - fd) <= 1e-3 * max(abs(fd), 1e-3 * np.abs(got).max()), (i, j, got[i, j], fd)
+
+
+def test_batched_rollout_equals_single_rollouts():
+    """rollout_batch (one stream per experiment, shared D and theta) gives the sums of the
+    single-experiment gradients."""
+    _gpu()
+    from cardiax_gb300.adjoint import rollout, rollout_batch
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    dev = torch.device("cuda", 0)
+    shape = (40, 52)
+    cases = [_case(shape, s) for s in (21, 22, 23)]
+    D = torch.tensor(cases[0][3], dtype=torch.float32, device=dev, requires_grad=True)
+    th = torch.tensor(P3[:13], dtype=torch.float32, device=dev, requires_grad=True)
+    s0 = torch.tensor(np.stack([np.stack(c[:3]) for c in cases]), dtype=torch.float32, device=dev)
+    stims = [[Stimulus(Protocol(*c[4][:3]), c[4][3].astype(np.float32))] for c in cases]
+    obs = cases[0][5]
+    R = torch.tensor(np.stack([c[6] for c in cases]), dtype=torch.float32, device=dev)
+    out = rollout_batch(s0, D, th, stims, 0, max(obs), obs)
+    (out * R).sum().backward()
+    gD_b, gth_b = D.grad.clone(), th.grad.clone()
+    D.grad = None
+    th.grad = None
+    total = 0
+    for b in range(3):
+        o = rollout(s0[b, 0], s0[b, 1], s0[b, 2], D, th, stims[b], 0, max(obs), obs)
+        total = total + (o * R[b]).sum()
+    total.backward()
+    torch.testing.assert_close(gD_b, D.grad, rtol=1e-5, atol=1e-9)
+    torch.testing.assert_close(gth_b, th.grad, rtol=1e-5, atol=1e-6)
