@@ -74,6 +74,11 @@ _SIGNATURES = {
     "fk_forward_euler_tracked": [Grid, _P, _P, _P, ctypes.POINTER(Params),
                                  ctypes.POINTER(Stimulus), _INT, _I64, _I64, _D, _D,
                                  ctypes.POINTER(Activation), _P],
+    "fk_forward_euler_flow": [Grid, _P, _P, _P, _P, ctypes.POINTER(Params),
+                              ctypes.POINTER(Stimulus), _INT, _I64, _I64, _D, _D,
+                              ctypes.POINTER(Activation), _P, _I64, _P],
+    "fk_forward_flow": [Grid, _P, _P, _P, ctypes.POINTER(Params), ctypes.POINTER(Stimulus), _INT,
+                        ctypes.POINTER(_I64), _INT, _D, _D, _P, _P, _I64, _P],
     "fk_heun_step": [Grid, _P, _P, ctypes.POINTER(Params), ctypes.POINTER(Stimulus), _INT, _I64,
                      _D, _D, _P, _P, _P],
     "fk_forward_heun": [Grid, _P, _P, _P, ctypes.POINTER(Params), ctypes.POINTER(Stimulus), _INT,
@@ -107,6 +112,8 @@ def lib(build: bool = True):
                 fn.argtypes = args
             L.fk_batch_workspace_bytes.restype = ctypes.c_size_t
             L.fk_batch_workspace_bytes.argtypes = [ctypes.POINTER(TissueDesc), _INT]
+            L.fk_flow_flag_words.restype = _I64
+            L.fk_flow_flag_words.argtypes = [Grid]
             _lib = L
     return _lib
 
@@ -118,4 +125,5 @@ def call(name: str, *args) -> None:
 
 
 def exported_symbols():
-    return ["fk_status_string", "fk_batch_workspace_bytes"] + list(_SIGNATURES)
+    return (["fk_status_string", "fk_batch_workspace_bytes", "fk_flow_flag_words"]
+            + list(_SIGNATURES))

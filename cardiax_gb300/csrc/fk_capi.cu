@@ -9,6 +9,8 @@
 //   fk_forward        cardiax/solve.py:168-222 forward (Euler integrator)
 //   fk_heun_step      cardiax/solve.py:73-85   step_heun
 //   fk_forward_heun   cardiax/solve.py:103-111 _forward_heun
+//   fk_forward_euler_flow, fk_forward_flow   _forward_euler / forward through the dataflow
+//                     kernel (one cooperative launch per call instead of one per step)
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
@@ -210,6 +212,96 @@ int step_once(const fk_grid &g, const float *in, float *out, const float *D, con
     return e == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
 
+// ---- dataflow stepping ------------------------------------------------------------------------
+static void fill_args(StepArgs &a, const fk_grid &g, const float *in, const float *D,
+                      const Model &m, const Stim *st, int ns, float dt, float rdx, int *status,
+                      const fk_activation *act) {
+    const int64_t plane = g.H * g.pitch;
+    a = StepArgs{};
+    a.v = in;
+    a.w = in + plane;
+    a.u = in + 2 * plane;
+    a.D = D;
+    a.H = (int)g.H;
+    a.W = (int)g.W;
+    a.pitch = (int)g.pitch;
+    a.dt = dt;
+    a.rdx = rdx;
+    a.n_stim = ns;
+    a.m = m;
+    for (int k = 0; k < ns; ++k) a.stim[k] = st[k];
+    a.status = status;
+    if (act) {
+        a.act_first = act->first;
+        a.act_last = act->last;
+        a.act_count = act->count;
+        a.act_threshold = act->threshold;
+    }
+}
+
+// Steps t0 .. t0+n-1 from `src` so that the last one lands in `dst` (src == dst allowed);
+// `scratch` is distinct from both.  Launches of at most 2^30 steps (the flags count steps in
+// int32).
+int flow_run(const fk_grid &g, const float *src, float *dst, float *scratch, const float *D,
+             const CUtensorMap &tm_d, const Model &m, const Stim *st, int ns, int64_t t0,
+             int64_t n, float dt, float rdx, const fk_activation *act, int32_t *flags,
+             int *status, cudaStream_t stream) {
+    const int64_t n_state = 3 * g.H * g.pitch;
+    if (n == 0) {
+        if (src != dst && cudaMemcpyAsync(dst, src, sizeof(float) * n_state,
+                                          cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+            return FK_ERR_CUDA;
+        return FK_OK;
+    }
+    const int64_t words = flow_flag_words(g.H, g.W);
+    const int64_t cap = (int64_t)1 << 30;
+    const float *cur = src;
+    for (int64_t done = 0; done < n;) {
+        const int64_t c = n - done < cap ? n - done : cap;  // cap is even
+        // step k writes bufs[k & 1]; the last writes bufs[(c-1) & 1]
+        float *bufs[2];
+        bool copy_back = false;
+        if (cur != dst) {
+            bufs[(c - 1) & 1] = dst;
+            bufs[c & 1] = scratch;
+        } else {  // in place: step 0 must not write its own input
+            bufs[0] = scratch;
+            bufs[1] = dst;
+            copy_back = (c & 1) != 0;
+        }
+        FlowMaps fm;
+        fm.d = tm_d;
+        FlowArgs fa;
+        const float *ins[3] = {cur, bufs[0], bufs[1]};
+        int rc;
+        for (int k = 0; k < 3; ++k) {
+            if ((rc = make_plane_map(&fm.uin[k], ins[k] + 2 * g.H * g.pitch, g.H, g.W, g.pitch,
+                                     SW, SU_H)))
+                return rc;
+            fill_args(fa.in[k], g, ins[k], D, m, st, ns, dt, rdx, status, act);
+        }
+        for (int b = 0; b < 2; ++b) {
+            const int64_t plane = g.H * g.pitch;
+            if ((rc = make_plane_map(&fm.ov[b], bufs[b], g.H, g.W, g.pitch, TX, TY)) ||
+                (rc = make_plane_map(&fm.ow[b], bufs[b] + plane, g.H, g.W, g.pitch, TX, TY)) ||
+                (rc = make_plane_map(&fm.ou[b], bufs[b] + 2 * plane, g.H, g.W, g.pitch, TX, TY)))
+                return rc;
+        }
+        fa.t0 = t0 + done;
+        fa.nsteps = (int)c;
+        fa.flags = flags;
+        if (cudaMemsetAsync(flags, 0, sizeof(int32_t) * words, stream) != cudaSuccess)
+            return FK_ERR_CUDA;
+        if (launch_flow(fm, fa, act != nullptr, stream) != cudaSuccess) return FK_ERR_CUDA;
+        if (copy_back && cudaMemcpyAsync(dst, scratch, sizeof(float) * n_state,
+                                         cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+            return FK_ERR_CUDA;
+        done += c;
+        cur = dst;
+    }
+    return FK_OK;
+}
+
 __global__ void add_state_kernel(float *dst, const float *src, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
@@ -353,6 +445,70 @@ int fk_forward_euler_tracked(fk_grid g, float *state, float *scratch, const floa
         if (cudaMemcpyAsync(state, scratch, sizeof(float) * 3 * g.H * g.pitch,
                             cudaMemcpyDeviceToDevice, s) != cudaSuccess)
             return FK_ERR_CUDA;
+    }
+    return FK_OK;
+}
+
+int64_t fk_flow_flag_words(fk_grid g) {
+    if (check_grid(g)) return -1;
+    return flow_flag_words(g.H, g.W);
+}
+
+int fk_forward_euler_flow(fk_grid g, const float *src, float *dst, float *scratch,
+                          const float *D, const fk_params *p, const fk_stimulus *stimuli,
+                          int n_stimuli, int64_t t0, int64_t t1, double dt, double dx,
+                          const fk_activation *act, int32_t *flags, int64_t n_flags,
+                          void *stream) {
+    int rc = common_checks(g, src, scratch, D, p, dx);
+    if (rc) return rc;
+    if (!dst || !flags) return FK_ERR_NULL;
+    if (!aligned16(dst)) return FK_ERR_ALIGN;
+    if (t1 < t0 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    if (scratch == src || scratch == dst) return FK_ERR_ARGUMENT;
+    if (n_flags < flow_flag_words(g.H, g.W)) return FK_ERR_ARGUMENT;
+    if (act) {
+        if (!act->first || !act->last || !act->count) return FK_ERR_NULL;
+        if (!std::isfinite(act->threshold)) return FK_ERR_ARGUMENT;
+    }
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
+    return flow_run(g, src, dst, scratch, D, tm_d, make_model(*p), st, n_stimuli, t0, t1 - t0,
+                    (float)dt, 1.0f / (float)dx, act, flags, status, (cudaStream_t)stream);
+}
+
+int fk_forward_flow(fk_grid g, const float *state0, float *scratch, const float *D,
+                    const fk_params *p, const fk_stimulus *stimuli, int n_stimuli,
+                    const int64_t *checkpoints, int n_checkpoints, double dt, double dx,
+                    float *out, int32_t *flags, int64_t n_flags, void *stream) {
+    int rc = common_checks(g, state0, scratch, D, p, dx);
+    if (rc) return rc;
+    if (!out || !checkpoints || !flags) return FK_ERR_NULL;
+    if (!aligned16(out)) return FK_ERR_ALIGN;
+    if (n_checkpoints < 1 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    if (n_flags < flow_flag_words(g.H, g.W)) return FK_ERR_ARGUMENT;
+    for (int i = 0; i + 1 < n_checkpoints; ++i)
+        if (checkpoints[i + 1] < checkpoints[i]) return FK_ERR_ARGUMENT;
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
+    const Model m = make_model(*p);
+    const int64_t n_state = 3 * g.H * g.pitch;
+    const float *cur = state0;
+    for (int i = 0; i + 1 < n_checkpoints; ++i) {
+        float *dst = out + (int64_t)i * n_state;
+        if (dst == scratch || cur == scratch) return FK_ERR_ARGUMENT;
+        if ((rc = flow_run(g, cur, dst, scratch, D, tm_d, m, st, n_stimuli, checkpoints[i],
+                           checkpoints[i + 1] - checkpoints[i], (float)dt, 1.0f / (float)dx,
+                           nullptr, flags, status, (cudaStream_t)stream)))
+            return rc;
+        cur = dst;
     }
     return FK_OK;
 }

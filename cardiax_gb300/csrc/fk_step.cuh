@@ -8,7 +8,7 @@
 
 namespace fk {
 
-// Tile geometry of the step kernel.  A persistent CTA of NT threads (one per SM) walks over
+// Tile geometry of the step kernel.  Persistent CTAs of NT threads (two per SM) walk over
 // TY x TX tiles with a three-stage TMA ring for the haloed u and D tiles (the loads of tiles
 // n+1 and n+2 are in flight while tile n is computed); v and w are read straight into
 // registers at the start of each tile, and the new state goes out through TMA stores from
@@ -16,13 +16,13 @@ namespace fk {
 //   pass 1: u_x on rows -2 .. TY+1 and u_y on columns -2 .. TX+1 go to shared memory;
 //   pass 2: thread (tx, ty) owns columns 4tx .. 4tx+3 of rows RPT*ty .. RPT*ty+RPT-1.
 #ifndef FK_TILE_X
-#define FK_TILE_X 128
+#define FK_TILE_X 64
 #endif
 #ifndef FK_TILE_Y
 #define FK_TILE_Y 32
 #endif
 #ifndef FK_THREADS
-#define FK_THREADS 512
+#define FK_THREADS 256
 #endif
 #ifndef FK_PASS1_UNROLL
 #define FK_PASS1_UNROLL 1
@@ -109,5 +109,29 @@ cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
 cudaError_t launch_add_int(int *p, int v, cudaStream_t stream);
 // Copies buffer 1 (scratch) of every tissue back to buffer 0 (state).
 cudaError_t launch_batch_copyback(const BatchTissue *tissues, int n_tissues, cudaStream_t stream);
+
+// ---- dataflow kernel: many steps of one tissue in one cooperative launch ----------------------
+// Step k of the launch reads `src` (k = 0) or buffer (k-1)&1 and writes buffer k&1.  Tile T of
+// step k starts once T and its eight neighbours have finished step k-1: each tile publishes the
+// number of steps it has completed in flags[T] (flags[ntiles] is an abort word).
+struct FlowMaps {
+    CUtensorMap d;
+    CUtensorMap uin[3];                  // u halo box of src, buffer 0, buffer 1
+    CUtensorMap ov[2], ow[2], ou[2];     // store boxes of buffer 0, buffer 1
+};
+struct FlowArgs {
+    StepArgs in[3];   // per input buffer (src, buffer 0, buffer 1): the planes read
+    int64_t t0;       // step index of the launch's first step
+    int nsteps;
+    int *flags;       // ntiles + 1 zeroed words
+};
+constexpr int SMEM_FLOW_BYTES = SMEM_STEP_BYTES + 2 * SMEM_ARGS_BYTES;
+// Number of int32 flag words the dataflow kernel needs for an H x W grid.
+inline int64_t flow_flag_words(int64_t H, int64_t W) {
+    return ((H + TY - 1) / TY) * ((W + TX - 1) / TX) + 1;
+}
+// Launches the dataflow kernel (cooperative: every CTA resident).  `act` selects activation
+// tracking (FlowArgs::in[*].act_* set).
+cudaError_t launch_flow(const FlowMaps &maps, const FlowArgs &a, bool act, cudaStream_t stream);
 
 }  // namespace fk

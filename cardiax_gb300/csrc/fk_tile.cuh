@@ -1,0 +1,517 @@
+// Tile-level device code shared by the step kernels (one launch per step, batched, dataflow):
+// the per-cell boundary path, the two-pass tile computation, TMA issue/store helpers.
+//
+// Reference semantics: cardiax/solve.py:26-70 (step + step_euler, with gradient x6, stimulate
+// and the edge pads fused).  Memory layout: SoA float32 planes, row pitch a multiple of 4
+// floats.
+//
+// Per tile: one TMA transaction brings the u tile with a 4-cell halo and the D tile with a
+// 2-row halo into shared memory (out-of-grid cells read as zero); v and w are read straight
+// into registers with 16-byte loads.  Each thread streams RPT rows of 4 columns:
+//   vertical derivatives   u_x, u_xx, D_x from register windows of shared-memory rows;
+//   horizontal derivatives u_y, u_yy, D_y from three 16-byte shared-memory reads per row.
+// Tiles that touch the grid edge clamp their halo to the reference's edge padding and pick
+// the one-sided stencil rows; one-row or one-column sliver tiles recompute the cells within 4
+// of an edge with a per-cell path that reads global memory with clamped indices.
+//
+// State planes are read with L2-coherent loads (ld.global.cg), never through the read-only
+// path: in the dataflow kernel they are rewritten by other CTAs while the kernel runs.
+#pragma once
+#include "fk_ptx.cuh"
+#include "fk_step.cuh"
+
+namespace fk {
+
+__device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+// ---- per-cell boundary path ---------------------------------------------------------------
+// Reads the input planes with the reference's edge padding: index -1 maps to 0, N to N-1.
+struct Clamped {
+    const float *p;
+    int H, W, pitch;
+    __device__ __forceinline__ float at(int r, int c) const {
+        return __ldcg(p + (int64_t)clampi(r, 0, H - 1) * pitch + clampi(c, 0, W - 1));
+    }
+};
+
+// d/dx of the padded u at padded row x in [-1, H] (cardiax/solve.py:225-254 along axis 0).
+__device__ __forceinline__ float ux_at(const Clamped &u, int x, int c) {
+    const int H = u.H;
+    if (x <= 0) return g_head(u.at(x, c), u.at(x + 1, c), u.at(x + 2, c), u.at(x + 3, c));
+    if (x >= H - 1) return g_tail(u.at(x - 3, c), u.at(x - 2, c), u.at(x - 1, c), u.at(x, c));
+    return g_central(u.at(x - 2, c), u.at(x - 1, c), u.at(x + 1, c), u.at(x + 2, c));
+}
+__device__ __forceinline__ float uy_at(const Clamped &u, int r, int y) {
+    const int W = u.W;
+    if (y <= 0) return g_head(u.at(r, y), u.at(r, y + 1), u.at(r, y + 2), u.at(r, y + 3));
+    if (y >= W - 1) return g_tail(u.at(r, y - 3), u.at(r, y - 2), u.at(r, y - 1), u.at(r, y));
+    return g_central(u.at(r, y - 2), u.at(r, y - 1), u.at(r, y + 1), u.at(r, y + 2));
+}
+
+// Activation bookkeeping for one cell (only touches memory on an upstroke).
+__device__ __forceinline__ void record_activation(const StepArgs &a, float t, int64_t off,
+                                                  float u_old, float u_new) {
+    if (u_old < a.act_threshold && u_new >= a.act_threshold) {
+        // through L2 (.cg): successive steps of a cell may run on different SMs
+        const int32_t t1 = (int32_t)t + 1;
+        __stcg(a.act_last + off, t1);
+        if (__ldcg(a.act_first + off) < 0) __stcg(a.act_first + off, t1);
+        __stcg(a.act_count + off, __ldcg(a.act_count + off) + 1);
+    }
+}
+
+// Output tile in shared memory (dense TY x TX per plane) that the TMA stores write out.
+struct OutTile {
+    float *v, *w, *u;
+    int i0, j0;
+};
+
+template <bool ACT>
+__device__ __noinline__ void boundary_cell(const StepArgs &a, float t, unsigned active, bool deriv,
+                                           int i, int j, const OutTile &o) {
+    const Clamped U{a.u, a.H, a.W, a.pitch}, D{a.D, a.H, a.W, a.pitch};
+    const int H = a.H, W = a.W;
+    const float rdx = a.rdx;
+    // first derivatives (scaled) at the padded positions the second derivative needs
+    auto UX = [&](int x) { return ux_at(U, x, j) * rdx; };
+    auto UY = [&](int y) { return uy_at(U, i, y) * rdx; };
+    float uxx, uyy, dxD, dyD;
+    if (i == 0) uxx = g_head(UX(0), UX(1), UX(2), UX(3));
+    else if (i == H - 1) uxx = g_tail(UX(H - 4), UX(H - 3), UX(H - 2), UX(H - 1));
+    else uxx = g_central(UX(i - 2), UX(i - 1), UX(i + 1), UX(i + 2));
+    if (j == 0) uyy = g_head(UY(0), UY(1), UY(2), UY(3));
+    else if (j == W - 1) uyy = g_tail(UY(W - 4), UY(W - 3), UY(W - 2), UY(W - 1));
+    else uyy = g_central(UY(j - 2), UY(j - 1), UY(j + 1), UY(j + 2));
+    uxx *= rdx;
+    uyy *= rdx;
+    if (i == 0) dxD = g_head(D.at(0, j), D.at(1, j), D.at(2, j), D.at(3, j));
+    else if (i == H - 1) dxD = g_tail(D.at(i - 3, j), D.at(i - 2, j), D.at(i - 1, j), D.at(i, j));
+    else dxD = g_central(D.at(i - 2, j), D.at(i - 1, j), D.at(i + 1, j), D.at(i + 2, j));
+    if (j == 0) dyD = g_head(D.at(i, 0), D.at(i, 1), D.at(i, 2), D.at(i, 3));
+    else if (j == W - 1) dyD = g_tail(D.at(i, j - 3), D.at(i, j - 2), D.at(i, j - 1), D.at(i, j));
+    else dyD = g_central(D.at(i, j - 2), D.at(i, j - 1), D.at(i, j + 1), D.at(i, j + 2));
+    dxD *= rdx;
+    dyD *= rdx;
+    const int64_t off = (int64_t)i * a.pitch + j;
+    const float u = __ldcg(a.u + off), v = __ldcg(a.v + off), w = __ldcg(a.w + off),
+                d = __ldg(a.D + off);
+    Reaction r = reaction(u, v, w, a.m);
+    if (active) {
+        float acc = 0.0f;
+        for (int s = 0; s < a.n_stim; ++s) {
+            if (!((active >> s) & 1u)) continue;
+            const Stim &st = a.stim[s];
+            float f = st.field ? __ldg(st.field + off)
+                               : ((i >= st.r0 && i < st.r1 && j >= st.c0 && j < st.c1) ? st.amplitude : 0.0f);
+            if (f != 0.0f) acc = f;
+        }
+        if (acc != 0.0f) r.j_ion = acc;
+    }
+    const float du = diffusion(d, dxD, dyD, UX(i), UY(j), uxx, uyy) + r.j_ion;
+    const int lo = (i - o.i0) * TX + (j - o.j0);
+    if (deriv) {
+        o.v[lo] = r.dv;
+        o.w[lo] = r.dw;
+        o.u[lo] = du;
+    } else {
+        o.v[lo] = fmaf(r.dv, a.dt, v);
+        o.w[lo] = fmaf(r.dw, a.dt, w);
+        const float un = fmaf(du, a.dt, u);
+        o.u[lo] = un;
+        if (ACT) record_activation(a, t, off, u, un);
+    }
+}
+
+// Stimulus override for the 4 cells (i, j .. j+3) of one thread: later active stimuli win,
+// a zero value leaves the ionic current (cardiax/solve.py:257-271).  Out of line: it runs only
+// on the steps where some protocol is on.
+static __device__ __noinline__ float4 apply_stimuli(const StepArgs &a, unsigned active, int i, int j,
+                                                    int64_t goff, float4 jion4) {
+    float j_ion[4] = {jion4.x, jion4.y, jion4.z, jion4.w};
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int jj = j + m;
+        if (i >= a.H || jj >= a.W) continue;
+        float acc = 0.0f;
+        for (int s = 0; s < a.n_stim; ++s) {
+            if (!((active >> s) & 1u)) continue;
+            const Stim &st = a.stim[s];
+            const float fv = st.field ? __ldg(st.field + goff + m)
+                                      : ((i >= st.r0 && i < st.r1 && jj >= st.c0 && jj < st.c1)
+                                             ? st.amplitude : 0.0f);
+            if (fv != 0.0f) acc = fv;
+        }
+        if (acc != 0.0f) j_ion[m] = acc;
+    }
+    return make_float4(j_ion[0], j_ion[1], j_ion[2], j_ion[3]);
+}
+
+// Cells of tile (i0, j0) within BAND of an edge, enumerated compactly so that each thread
+// takes ceil(count / NT) of them: a top strip, a bottom strip, and left/right strips between.
+template <bool ACT>
+__device__ __noinline__ void boundary_band(const StepArgs &a, float t, unsigned active, bool deriv,
+                                           int i0, int j0, const OutTile &o) {
+    const int H = a.H, W = a.W;
+    const int i1 = min(i0 + TY, H), j1 = min(j0 + TX, W);
+    const int jw = j1 - j0;
+    // interior rectangle of the tile (may be empty)
+    const int ri0 = min(max(i0, BAND), i1), ri1 = max(min(i1, H - BAND), ri0);
+    const int rj0 = min(max(j0, BAND), j1), rj1 = max(min(j1, W - BAND), rj0);
+    const int n_top = (ri0 - i0) * jw, n_bot = (i1 - ri1) * jw;
+    const int wl = rj0 - j0, wr = j1 - rj1, n_mid = (ri1 - ri0) * (wl + wr);
+    const int total = n_top + n_bot + n_mid;
+    for (int idx = threadIdx.x; idx < total; idx += NT) {
+        int i, j;
+        if (idx < n_top) {
+            i = i0 + idx / jw;
+            j = j0 + idx % jw;
+        } else if (idx < n_top + n_bot) {
+            const int k = idx - n_top;
+            i = ri1 + k / jw;
+            j = j0 + k % jw;
+        } else {
+            const int k = idx - n_top - n_bot;
+            const int r = k / (wl + wr), c = k % (wl + wr);
+            i = ri0 + r;
+            j = c < wl ? j0 + c : rj1 + (c - wl);
+        }
+        boundary_cell<ACT>(a, t, active, deriv, i, j, o);
+    }
+}
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, float4 v) { *reinterpret_cast<float4 *>(p) = v; }
+
+// Shared-memory buffers of one pipeline stage (the haloed u and D tiles), and the tile's own
+// v, w values (registers, loaded at the start of the tile) and output tiles.
+struct Stage {
+    float *u, *d;
+};
+struct TileIO {
+    float4 v[RPT], w[RPT];   // input v, w of this thread's pass-2 cells
+    float *ov, *ow, *ou;     // dense output tiles
+};
+
+__device__ __forceinline__ Stage stage_at(unsigned char *base, int s) {
+    unsigned char *p = base + s * SMEM_STAGE_BYTES;
+    Stage st;
+    st.u = reinterpret_cast<float *>(p);
+    st.d = reinterpret_cast<float *>(p + SMEM_U_BYTES);
+    return st;
+}
+
+__device__ __forceinline__ void issue_tile(const CUtensorMap *u, const CUtensorMap *d,
+                                           const Stage &st, uint64_t *bar, int i0, int j0) {
+    mbar_arrive_expect_tx(bar, SMEM_STAGE_BYTES);
+    tma_load_2d(st.u, u, j0 - HALO_U, i0 - HALO_U, bar);
+    tma_load_2d(st.d, d, j0 - HALO_U, i0 - HALO_D, bar);
+}
+__device__ __forceinline__ void issue_tile(const StepMaps &tm, const Stage &st, uint64_t *bar,
+                                           int i0, int j0) {
+    issue_tile(&tm.u, &tm.d, st, bar, i0, j0);
+}
+
+// This thread's v, w for pass 2 (16-byte loads, zero outside the grid).
+__device__ __forceinline__ void load_vw(const StepArgs &a, int i0, int j0, TileIO &io) {
+    const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
+    const int j = j0 + 4 * tx;
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+        const int i = i0 + RPT * ty + k;
+        io.v[k] = io.w[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < a.H && j < a.W) {
+            const int64_t off = (int64_t)i * a.pitch + j;
+            io.v[k] = __ldcg(reinterpret_cast<const float4 *>(a.v + off));
+            io.w[k] = __ldcg(reinterpret_cast<const float4 *>(a.w + off));
+        }
+    }
+}
+
+// Edge tiles: replace the zero fill of the out-of-grid halo by the reference's edge padding
+// (copies of the first/last row and column).  Only the 4 grid rows and columns beyond each edge
+// are rewritten: the stencils of in-grid cells read at most 2 beyond (u_x, u_y and D at rows /
+// columns -2 .. H+1 / W+1), and what is computed for out-of-grid cells is never stored.
+static __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_rows, int i0, int j0,
+                                               int H, int W) {
+    constexpr int SW4 = SW / 4;  // float4 per buffer row (rows are 16-byte aligned)
+    const int tid = threadIdx.x;
+    // rows -4 .. -1 take row 0, rows H .. H+3 take row H-1 (where they fall in the buffer)
+    for (int it = tid; it < 8 * SW4; it += NT) {
+        const int k = it / SW4, c4 = it % SW4;
+        const int gr = k < 4 ? k - 4 : H + (k - 4);
+        const int sr = gr - i0 + halo_rows;
+        if (sr < 0 || sr >= rows) continue;
+        const int src = (k < 4 ? 0 : H - 1) - i0 + halo_rows;
+        reinterpret_cast<float4 *>(buf + sr * SW)[c4] =
+            reinterpret_cast<const float4 *>(buf + src * SW)[c4];
+    }
+    __syncthreads();
+    // then columns -4 .. -1 and W .. W+3 (corners get the corner cell)
+    for (int it = tid; it < 8 * rows; it += NT) {
+        const int k = it & 7, sr = it >> 3;
+        const int gc = k < 4 ? k - 4 : W + (k - 4);
+        const int c = gc - j0 + HALO_U;
+        if (c < 0 || c >= SW) continue;
+        const int src = (k < 4 ? 0 : W - 1) - j0 + HALO_U;
+        buf[sr * SW + c] = buf[sr * SW + src];
+    }
+}
+
+// One tile: pass 1 (first derivatives into shared memory), pass 2 (everything else).
+// EDGE: the tile touches the grid edge (and is not a one-row or one-column sliver): the halo
+// is clamped and every derivative picks the reference's row type, exactly as the padded
+// arrays of cardiax/solve.py:29-32,49-54 do.
+template <bool DERIV, bool ACT, bool EDGE, class P1>
+__device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const Stage &st,
+                                             float *sux, float *suy, const TileIO &io,
+                                             unsigned active, int i0, int j0, P1 &&after_pass1) {
+    const int tid = threadIdx.x;
+    const int H = a.H, W = a.W, pitch = a.pitch;
+    const float rdx = a.rdx;
+    float *su = st.u, *sd = st.d;
+
+    if (EDGE) {
+        clamp_halo(su, SU_H, HALO_U, i0, j0, H, W);
+        clamp_halo(sd, SD_H, HALO_D, i0, j0, H, W);
+        __syncthreads();
+    }
+
+    // ---- pass 1: u_x (tile rows -2 .. TY+1) and u_y (tile columns -2 .. TX+1) -------------
+#pragma unroll PASS1_UNROLL
+    for (int it = tid; it < SUX_H * NTX; it += NT) {
+        const int r = it / NTX, q = it % NTX;
+        const float *b = su + (r + 2) * SW + HALO_U + 4 * q;  // u row of ux row r
+        float4 o;
+        if (!EDGE) {
+            o = g_central4(ld4(b - 2 * SW), ld4(b - SW), ld4(b + SW), ld4(b + 2 * SW));
+        } else {
+            const int x = i0 - 2 + r;  // global row of this u_x row
+            if (x <= 0)
+                o = [&] {
+                    const float4 a0 = ld4(b), a1 = ld4(b + SW), a2 = ld4(b + 2 * SW), a3 = ld4(b + 3 * SW);
+                    return make_float4(g_head(a0.x, a1.x, a2.x, a3.x), g_head(a0.y, a1.y, a2.y, a3.y),
+                                       g_head(a0.z, a1.z, a2.z, a3.z), g_head(a0.w, a1.w, a2.w, a3.w));
+                }();
+            else if (x >= H - 1)
+                o = [&] {
+                    const float4 a0 = ld4(b - 3 * SW), a1 = ld4(b - 2 * SW), a2 = ld4(b - SW), a3 = ld4(b);
+                    return make_float4(g_tail(a0.x, a1.x, a2.x, a3.x), g_tail(a0.y, a1.y, a2.y, a3.y),
+                                       g_tail(a0.z, a1.z, a2.z, a3.z), g_tail(a0.w, a1.w, a2.w, a3.w));
+                }();
+            else
+                o = g_central4(ld4(b - 2 * SW), ld4(b - SW), ld4(b + SW), ld4(b + 2 * SW));
+        }
+        st4(sux + r * TX + 4 * q, mul4(o, rdx));
+    }
+#pragma unroll PASS1_UNROLL
+    for (int it = tid; it < TY * NTX; it += NT) {
+        const int r = it / NTX, q = it % NTX;
+        const float *b = su + (r + HALO_U) * SW + 4 * q;  // columns j0+4q-4 .. j0+4q+7
+        const float4 x0 = ld4(b), x1 = ld4(b + 4), x2 = ld4(b + 8);
+        const float e[12] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
+                             x2.x, x2.y, x2.z, x2.w};
+        float o[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            if (!EDGE) {
+                o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
+            } else {  // u_y at padded position y: head / tail / central row of the padded line
+                const int y = j0 + 4 * q + m;
+                if (y <= 0) o[m] = g_head(e[m + 4], e[m + 5], e[m + 6], e[m + 7]);
+                else if (y >= W - 1) o[m] = g_tail(e[m + 1], e[m + 2], e[m + 3], e[m + 4]);
+                else o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
+            }
+        }
+        st4(suy + r * SW + HALO_U + 4 * q,
+            make_float4(o[0] * rdx, o[1] * rdx, o[2] * rdx, o[3] * rdx));
+    }
+    if (tid >= NT - TY * 4) {  // the 2 + 2 halo columns of u_y (threads with one ux item less)
+        const int h = tid - (NT - TY * 4);
+        const int r = h / 4, k = h % 4;
+        const int c = k < 2 ? 2 + k : TX + HALO_U + (k - 2);  // same column index in su and suy
+        const float *row = su + (r + HALO_U) * SW;
+        float o;
+        if (!EDGE) {
+            o = g_central(row[c - 2], row[c - 1], row[c + 1], row[c + 2]);
+        } else {
+            const int y = j0 - HALO_U + c;
+            if (y <= 0) o = g_head(row[c], row[c + 1], row[c + 2], row[c + 3]);
+            else if (y >= W - 1) o = g_tail(row[c - 3], row[c - 2], row[c - 1], row[c]);
+            else o = g_central(row[c - 2], row[c - 1], row[c + 1], row[c + 2]);
+        }
+        suy[r * SW + c] = o * rdx;
+    }
+    if (tid < 32) after_pass1();  // warp 0: e.g. free the output tiles, start further loads
+    __syncthreads();
+
+    // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
+    const int tx = tid % NTX, ty = tid / NTX;
+    const int j = j0 + 4 * tx;
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+        const int r = RPT * ty + k;
+        const int i = i0 + r;
+        const int64_t goff = (int64_t)i * pitch + j;
+        const float *xb = sux + (r + 2) * TX + 4 * tx;
+        const float4 uxc = ld4(xb);
+        const float *db = sd + (r + HALO_D) * SW + HALO_U + 4 * tx;
+        const float4 dc = ld4(db);
+        float4 uxx, dxD;
+        if (!EDGE || (i != 0 && i != H - 1)) {
+            uxx = g_central4(ld4(xb - 2 * TX), ld4(xb - TX), ld4(xb + TX), ld4(xb + 2 * TX));
+            dxD = g_central4(ld4(db - 2 * SW), ld4(db - SW), ld4(db + SW), ld4(db + 2 * SW));
+        } else if (i == 0) {  // head rows on u_x rows 0..3 and D rows 0..3
+            const float4 a0 = uxc, a1 = ld4(xb + TX), a2 = ld4(xb + 2 * TX), a3 = ld4(xb + 3 * TX);
+            uxx = make_float4(g_head(a0.x, a1.x, a2.x, a3.x), g_head(a0.y, a1.y, a2.y, a3.y),
+                              g_head(a0.z, a1.z, a2.z, a3.z), g_head(a0.w, a1.w, a2.w, a3.w));
+            const float4 b0 = dc, b1 = ld4(db + SW), b2 = ld4(db + 2 * SW), b3 = ld4(db + 3 * SW);
+            dxD = make_float4(g_head(b0.x, b1.x, b2.x, b3.x), g_head(b0.y, b1.y, b2.y, b3.y),
+                              g_head(b0.z, b1.z, b2.z, b3.z), g_head(b0.w, b1.w, b2.w, b3.w));
+        } else {  // i == H-1: tail rows on rows H-4 .. H-1
+            const float4 a0 = ld4(xb - 3 * TX), a1 = ld4(xb - 2 * TX), a2 = ld4(xb - TX), a3 = uxc;
+            uxx = make_float4(g_tail(a0.x, a1.x, a2.x, a3.x), g_tail(a0.y, a1.y, a2.y, a3.y),
+                              g_tail(a0.z, a1.z, a2.z, a3.z), g_tail(a0.w, a1.w, a2.w, a3.w));
+            const float4 b0 = ld4(db - 3 * SW), b1 = ld4(db - 2 * SW), b2 = ld4(db - SW), b3 = dc;
+            dxD = make_float4(g_tail(b0.x, b1.x, b2.x, b3.x), g_tail(b0.y, b1.y, b2.y, b3.y),
+                              g_tail(b0.z, b1.z, b2.z, b3.z), g_tail(b0.w, b1.w, b2.w, b3.w));
+        }
+        uxx = mul4(uxx, rdx);
+        dxD = mul4(dxD, rdx);
+        const float *yb = suy + r * SW + 4 * tx;
+        const float4 y0 = ld4(yb), y1 = ld4(yb + 4), y2 = ld4(yb + 8);
+        const float4 dl = ld4(db - 4), dr = ld4(db + 4);
+        const float4 uc = ld4(su + (r + HALO_U) * SW + HALO_U + 4 * tx);
+        const float4 vc = io.v[k], wc = io.w[k];
+
+        const float f[12] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w,
+                             y2.x, y2.y, y2.z, y2.w};
+        const float g[12] = {dl.x, dl.y, dl.z, dl.w, dc.x, dc.y, dc.z, dc.w,
+                             dr.x, dr.y, dr.z, dr.w};
+        const float uu[4] = {uc.x, uc.y, uc.z, uc.w};
+        const float vv[4] = {vc.x, vc.y, vc.z, vc.w};
+        const float ww[4] = {wc.x, wc.y, wc.z, wc.w};
+        const float dd[4] = {dc.x, dc.y, dc.z, dc.w};
+        const float dxv[4] = {dxD.x, dxD.y, dxD.z, dxD.w};
+        const float uxv[4] = {uxc.x, uxc.y, uxc.z, uxc.w};
+        const float uxxv[4] = {uxx.x, uxx.y, uxx.z, uxx.w};
+        float ov[4], ow[4], ou[4], jion[4], dv[4], dw[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const Reaction re = reaction(uu[m], vv[m], ww[m], a.m);
+            jion[m] = re.j_ion;
+            dv[m] = re.dv;
+            dw[m] = re.dw;
+        }
+        if (active) {
+            const float4 js = apply_stimuli(a, active, i, j, goff,
+                                            make_float4(jion[0], jion[1], jion[2], jion[3]));
+            jion[0] = js.x;
+            jion[1] = js.y;
+            jion[2] = js.z;
+            jion[3] = js.w;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            float uyy, dyD;
+            if (!EDGE) {
+                uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
+                dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
+            } else {  // second derivative / D_y at column y: head at 0, tail at W-1
+                const int y = j + m;
+                if (y == 0) {
+                    uyy = g_head(f[m + 4], f[m + 5], f[m + 6], f[m + 7]);
+                    dyD = g_head(g[m + 4], g[m + 5], g[m + 6], g[m + 7]);
+                } else if (y == W - 1) {
+                    uyy = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]);
+                    dyD = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]);
+                } else {
+                    uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
+                    dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
+                }
+            }
+            uyy *= rdx;
+            dyD *= rdx;
+            const float du = diffusion(dd[m], dxv[m], dyD, uxv[m], f[m + 4], uxxv[m], uyy) + jion[m];
+            if (DERIV) {
+                ov[m] = dv[m];
+                ow[m] = dw[m];
+                ou[m] = du;
+            } else {
+                ov[m] = fmaf(dv[m], a.dt, vv[m]);
+                ow[m] = fmaf(dw[m], a.dt, ww[m]);
+                ou[m] = fmaf(du, a.dt, uu[m]);
+            }
+        }
+        st4(io.ov + r * TX + 4 * tx, make_float4(ov[0], ov[1], ov[2], ov[3]));
+        st4(io.ow + r * TX + 4 * tx, make_float4(ow[0], ow[1], ow[2], ow[3]));
+        st4(io.ou + r * TX + 4 * tx, make_float4(ou[0], ou[1], ou[2], ou[3]));
+        if (ACT && !DERIV && i < H) {
+#pragma unroll
+            for (int m = 0; m < 4; ++m)
+                if (j + m < W) record_activation(a, t, goff + m, uu[m], ou[m]);
+        }
+    }
+}
+
+// A tile that needs the per-cell boundary path: the last row or column of tiles holds a
+// single grid row or column (too few rows in the tile for the one-sided stencils).
+__device__ __forceinline__ bool is_sliver(int i0, int j0, int H, int W) {
+    return H - i0 < 2 || W - j0 < 2;
+}
+
+// Interior tiles, clamped edge tiles, or slivers (interior passes + per-cell band).
+template <bool DERIV, bool ACT, class P1>
+__device__ __forceinline__ void process_tile(const StepArgs &a, float t, const Stage &st,
+                                             float *sux, float *suy, const TileIO &io,
+                                             unsigned active, int i0, int j0, P1 &&after_pass1) {
+    const int H = a.H, W = a.W;
+    const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
+    if (interior) {
+        compute_tile<DERIV, ACT, false>(a, t, st, sux, suy, io, active, i0, j0, after_pass1);
+    } else if (!is_sliver(i0, j0, H, W)) {
+        compute_tile<DERIV, ACT, true>(a, t, st, sux, suy, io, active, i0, j0, after_pass1);
+    } else {
+        compute_tile<DERIV, false, false>(a, t, st, sux, suy, io, active, i0, j0, after_pass1);
+        __syncthreads();  // every cell of this tile is recomputed below where needed
+        boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0,
+                                     OutTile{io.ov, io.ow, io.ou, i0, j0});
+        if (ACT && !DERIV) {  // interior cells of the sliver tile: record from the tile values
+            const int tid = threadIdx.x;
+            for (int idx = tid; idx < TY * TX; idx += NT) {
+                const int i = i0 + idx / TX, j = j0 + idx % TX;
+                if (i >= BAND && i < H - BAND && j >= BAND && j < W - BAND)
+                    record_activation(a, t, (int64_t)i * a.pitch + j,
+                                      st.u[(idx / TX + HALO_U) * SW + HALO_U + idx % TX],
+                                      io.ou[idx]);
+            }
+        }
+    }
+}
+
+// Writes the output tiles with TMA stores (after all threads have written them).
+__device__ __forceinline__ void store_tile(const CUtensorMap *ov, const CUtensorMap *ow,
+                                           const CUtensorMap *ou, const TileIO &io, int i0,
+                                           int j0) {
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tma_store_2d(ov, io.ov, j0, i0);
+        tma_store_2d(ow, io.ow, j0, i0);
+        tma_store_2d(ou, io.ou, j0, i0);
+        bulk_commit();
+    }
+}
+__device__ __forceinline__ void store_tile(const StepMaps &tm, const TileIO &io, int i0, int j0) {
+    store_tile(&tm.ov, &tm.ow, &tm.ou, io, i0, j0);
+}
+
+static_assert(sizeof(StepArgs) <= SMEM_ARGS_BYTES, "StepArgs does not fit its shared slot");
+
+// Copies a StepArgs into shared memory (all threads; a barrier must follow).
+__device__ __forceinline__ void stage_args(StepArgs *dst, const StepArgs *src) {
+    const uint32_t *s = reinterpret_cast<const uint32_t *>(src);
+    uint32_t *d = reinterpret_cast<uint32_t *>(dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(StepArgs) / 4); k += NT) d[k] = s[k];
+}
+
+}  // namespace fk

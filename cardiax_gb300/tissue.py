@@ -172,12 +172,32 @@ class Tissue:
         return self.act_first[:, :W], self.act_last[:, :W], self.act_count[:, :W]
 
     # -- stepping -------------------------------------------------------------------------
-    def advance(self, t0: int, t1: int) -> "Tissue":
-        """Steps t0 .. t1-1 in place (cardiax/solve.py:92-100)."""
+    def _flow_flags(self) -> torch.Tensor:
+        """Tile-progress words of the dataflow kernel (owned by this tissue; its calls are
+        ordered on one stream)."""
+        if getattr(self, "_flags", None) is None:
+            n = int(N.lib().fk_flow_flag_words(self.grid))
+            self._flags = torch.zeros(n, dtype=torch.int32, device=self.device)
+        return self._flags
+
+    def advance(self, t0: int, t1: int, schedule: str = "step") -> "Tissue":
+        """Steps t0 .. t1-1 in place (cardiax/solve.py:92-100).  ``schedule="step"``: one launch
+        per step (chained with programmatic dependent launch); ``"flow"``: one cooperative
+        dataflow launch for the whole range.  Both give identical results."""
         act = ctypes.byref(self.activation) if self.activation is not None else None
-        N.call("fk_forward_euler_tracked", self.grid, self.state.data_ptr(),
+        if schedule == "step":
+            N.call("fk_forward_euler_tracked", self.grid, self.state.data_ptr(),
+                   self.scratch.data_ptr(), self.D.data_ptr(), ctypes.byref(self.params),
+                   self.stim, self.n_stim, int(t0), int(t1), self.dt, self.dx, act,
+                   stream_handle())
+            return self
+        if schedule != "flow":
+            raise ValueError(f"unknown schedule {schedule!r}")
+        flags = self._flow_flags()
+        N.call("fk_forward_euler_flow", self.grid, self.state.data_ptr(), self.state.data_ptr(),
                self.scratch.data_ptr(), self.D.data_ptr(), ctypes.byref(self.params), self.stim,
-               self.n_stim, int(t0), int(t1), self.dt, self.dx, act, stream_handle())
+               self.n_stim, int(t0), int(t1), self.dt, self.dx, act, flags.data_ptr(),
+               flags.numel(), stream_handle())
         return self
 
     def advance_heun(self, t0: int, t1: int) -> "Tissue":
@@ -190,10 +210,11 @@ class Tissue:
                int(t1), self.dt, self.dx, stream_handle())
         return self
 
-    def forward(self, checkpoints, out: torch.Tensor = None) -> torch.Tensor:
+    def forward(self, checkpoints, out: torch.Tensor = None,
+                schedule: str = "step") -> torch.Tensor:
         """States at checkpoints[1:] starting from the current state, as a
         (len-1, 3, H, pitch) tensor (cardiax/solve.py:168-222).  The current state is not
-        modified."""
+        modified.  ``schedule`` as in :meth:`advance`."""
         ck = [int(_scalar(c)) for c in checkpoints]
         n = max(0, len(ck) - 1)
         if out is None:
@@ -202,9 +223,18 @@ class Tissue:
         if n == 0:
             return out
         arr = (ctypes.c_int64 * len(ck))(*ck)
-        N.call("fk_forward", self.grid, self.state.data_ptr(), self.scratch.data_ptr(),
+        if schedule == "step":
+            N.call("fk_forward", self.grid, self.state.data_ptr(), self.scratch.data_ptr(),
+                   self.D.data_ptr(), ctypes.byref(self.params), self.stim, self.n_stim, arr,
+                   len(ck), self.dt, self.dx, out.data_ptr(), stream_handle())
+            return out
+        if schedule != "flow":
+            raise ValueError(f"unknown schedule {schedule!r}")
+        flags = self._flow_flags()
+        N.call("fk_forward_flow", self.grid, self.state.data_ptr(), self.scratch.data_ptr(),
                self.D.data_ptr(), ctypes.byref(self.params), self.stim, self.n_stim, arr,
-               len(ck), self.dt, self.dx, out.data_ptr(), stream_handle())
+               len(ck), self.dt, self.dx, out.data_ptr(), flags.data_ptr(), flags.numel(),
+               stream_handle())
         return out
 
     def derivative(self, t: int, out: torch.Tensor = None) -> torch.Tensor:

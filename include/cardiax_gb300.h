@@ -142,10 +142,31 @@ int fk_forward_euler_tracked(fk_grid g, float *state, float *scratch, const floa
                              int64_t t0, int64_t t1, double dt, double dx,
                              const fk_activation *act, void *stream);
 
+/* Dataflow stepping: fk_forward_euler_tracked and fk_forward in one cooperative launch per call
+ * instead of one launch per step (no reference counterpart; same results bit for bit).  Tile T of
+ * step t starts as soon as T and its eight neighbours have finished step t-1, tracked in
+ * `flags`: an int32 device array of at least fk_flow_flag_words(g) words owned by the call
+ * (zeroed by the call on `stream`; calls that overlap on the GPU need separate arrays). */
+int64_t fk_flow_flag_words(fk_grid g);
+
+/* Steps t0 .. t1-1 from `src` into `dst` (src == dst: in place); `scratch` is a third state
+ * buffer (distinct from src and dst) and `act` may be NULL. */
+int fk_forward_euler_flow(fk_grid g, const float *src, float *dst, float *scratch,
+                          const float *D, const fk_params *p, const fk_stimulus *stimuli,
+                          int n_stimuli, int64_t t0, int64_t t1, double dt, double dx,
+                          const fk_activation *act, int32_t *flags, int64_t n_flags,
+                          void *stream);
+
+/* fk_forward through the dataflow kernel (one launch per checkpoint interval). */
+int fk_forward_flow(fk_grid g, const float *state0, float *scratch, const float *D,
+                    const fk_params *p, const fk_stimulus *stimuli, int n_stimuli,
+                    const int64_t *checkpoints, int n_checkpoints, double dt, double dx,
+                    float *out, int32_t *flags, int64_t n_flags, void *stream);
+
 /* ---- many tissues in one launch --------------------------------------------------------------
  * No reference counterpart: the reference steps one tissue per call (its data generation loops
  * over tissues in Python, deepx/generate.py:135-210).  Here every tissue of a batch advances in
- * one persistent kernel per step that drains a list of 32x128 tiles of all tissues, and runs of
+ * one persistent kernel per step that drains a list of tiles of all tissues, and runs of
  * steps are replayed from a captured CUDA graph.  Tissues may differ in shape, parameters, D,
  * stimuli and dt/dx; they advance through the same step indices. */
 typedef struct {

@@ -151,5 +151,7 @@ def test_batched_rollout_equals_single_rollouts():
         o = rollout(s0[b, 0], s0[b, 1], s0[b, 2], D, th, stims[b], 0, max(obs), obs)
         total = total + (o * R[b]).sum()
     total.backward()
-    torch.testing.assert_close(gD_b, D.grad, rtol=1e-5, atol=1e-9)
-    torch.testing.assert_close(gth_b, th.grad, rtol=1e-5, atol=1e-6)
+    # the per-experiment gradients are summed in a different order (float32): compare relative
+    # to the largest entry, as cancellation leaves a few entries near zero
+    torch.testing.assert_close(gD_b, D.grad, rtol=1e-5, atol=1e-5 * D.grad.abs().max().item())
+    torch.testing.assert_close(gth_b, th.grad, rtol=1e-5, atol=1e-5 * th.grad.abs().max().item())
