@@ -16,6 +16,9 @@ amplitude 20, Protocol(start=0, duration=200, period=20000) in steps), advanced 
                    per cell-update (read u, v, w, D; write u, v, w).
 * ``cpu_baseline`` the C restatement of the reference's stepper (the oracle port) on the host's
                    cores, on a bounded sample of the same workload.
+* ``schedules``    the roofline workload at 1024^2 and 2048^2 (a few hundred steps each) under
+                   every schedule: one launch per step (k = 1), temporal blocking with k = 2, 4,
+                   8 steps per launch, and the dataflow launch; all give identical bits.
 
 ``--impl reference`` times that CPU implementation alone on the same workload (the reference's
 own JAX CPU path cannot be installed here; the port is its restatement).  Multi-GPU runs are
@@ -340,6 +343,42 @@ def run_reference(args):
 METRIC = "GCUPS (1e9 Fenton-Karma cell-updates/s), fused FP32 Euler stepper; roofline.frac = % of HBM roofline"
 
 
+def run_schedules(dev, sizes=(1024, 2048), steps: int = 400):
+    """GCUPS of each stepping schedule on the roofline workload (best of 2 runs of ``steps``
+    steps, L2 flushed before each run)."""
+    import torch
+    from cardiax_gb300 import params
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    from cardiax_gb300.tissue import Tissue
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    modes = {"k1": {}, "k2": {"depth": 2}, "k4": {"depth": 4}, "k8": {"depth": 8},
+             "flow": {"schedule": "flow"}}
+    out = {}
+    for size in sizes:
+        D, field, proto = workload(size, size)
+        tis = Tissue((size, size), params.PARAMSET_3, D, [Stimulus(Protocol(*proto), field)],
+                     device=dev)
+        row = {}
+        for name, kw in modes.items():
+            tis.init()
+            tis.advance(0, 16, **kw)  # warm-up (kernel attributes, maps)
+            best = None
+            for rep in range(2):
+                flush.fill_(float(rep))
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                tis.advance(16 + rep * steps, 16 + (rep + 1) * steps, **kw)
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+                best = ms if best is None else min(best, ms)
+            row[name] = {"gcups": size * size * steps / (best / 1e3) / 1e9,
+                         "us_per_step": best * 1e3 / steps}
+        out[f"{size}x{size}"] = row
+    return out
+
+
 def config(args):
     return {"workload": f"roofline_{args.size}: {args.size}x{args.size} FP32, PARAMSET_3, "
                         f"D=0.001(1+0.05n) clipped>=0, n=N(0,1) smoothed over 2 cells, "
@@ -450,6 +489,9 @@ def run_ours(args):
     adjoint = None
     if not args.no_adjoint:
         adjoint = run_adjoint(dev)
+    schedules = None
+    if not args.no_schedules:
+        schedules = run_schedules(dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -465,7 +507,8 @@ def run_ours(args):
                "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
                "config": config(args), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-               "gpu_launches": args.steps * (S + 1), "clocks": clk, "batched": batched, "adjoint": adjoint,
+               "gpu_launches": args.steps * (S + 1), "clocks": clk, "batched": batched,
+               "adjoint": adjoint, "schedules": schedules,
                "wall_s_timed_region": t_wall}
         print(json.dumps(out))
     if world > 1:
@@ -487,6 +530,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-schedules", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=2000)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -77,6 +77,8 @@ _SIGNATURES = {
     "fk_forward_euler_flow": [Grid, _P, _P, _P, _P, ctypes.POINTER(Params),
                               ctypes.POINTER(Stimulus), _INT, _I64, _I64, _D, _D,
                               ctypes.POINTER(Activation), _P, _I64, _P],
+    "fk_forward_euler_tb": [Grid, _P, _P, _P, ctypes.POINTER(Params), ctypes.POINTER(Stimulus),
+                            _INT, _I64, _I64, _D, _D, _INT, _P],
     "fk_forward_flow": [Grid, _P, _P, _P, ctypes.POINTER(Params), ctypes.POINTER(Stimulus), _INT,
                         ctypes.POINTER(_I64), _INT, _D, _D, _P, _P, _I64, _P],
     "fk_heun_step": [Grid, _P, _P, ctypes.POINTER(Params), ctypes.POINTER(Stimulus), _INT, _I64,

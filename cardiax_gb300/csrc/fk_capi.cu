@@ -11,6 +11,7 @@
 //   fk_forward_heun   cardiax/solve.py:103-111 _forward_heun
 //   fk_forward_euler_flow, fk_forward_flow   _forward_euler / forward through the dataflow
 //                     kernel (one cooperative launch per call instead of one per step)
+//   fk_forward_euler_tb   _forward_euler with `depth` steps per launch (temporal blocking)
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
@@ -24,6 +25,7 @@
 #include "fk_capi_internal.h"
 #include "fk_adjoint.cuh"
 #include "fk_step.cuh"
+#include "fk_tb.cuh"
 
 namespace fk {
 
@@ -510,6 +512,66 @@ int fk_forward_flow(fk_grid g, const float *state0, float *scratch, const float 
             return rc;
         cur = dst;
     }
+    return FK_OK;
+}
+
+int fk_forward_euler_tb(fk_grid g, float *state, float *scratch, const float *D,
+                        const fk_params *p, const fk_stimulus *stimuli, int n_stimuli, int64_t t0,
+                        int64_t t1, double dt, double dx, int depth, void *stream) {
+    int rc = common_checks(g, state, scratch, D, p, dx);
+    if (rc) return rc;
+    if (t1 < t0 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    if (depth != 1 && depth != 2 && depth != 4 && depth != 8) return FK_ERR_ARGUMENT;
+    int bw = 0, bh = 0, ow = 0, oh = 0;
+    tb_box(depth, &bw, &bh, &ow, &oh);
+    // one-cell last tile row/column: the one-sided rows reach beyond the blocked halo
+    if (depth == 1 || g.H % oh == 1 || g.W % ow == 1)
+        return fk_forward_euler(g, state, scratch, D, p, stimuli, n_stimuli, t0, t1, dt, dx,
+                                stream);
+    Stim st[kMaxStim];
+    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    int *status = status_ptr();
+    if (!status) return FK_ERR_CUDA;
+    const Model m = make_model(*p);
+    const float rdx = 1.0f / (float)dx;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t plane = g.H * g.pitch;
+    float *bufs[2] = {state, scratch};
+    TbMaps tm[2];  // tm[k]: reads bufs[k], writes bufs[k^1]
+    CUtensorMap dmap;
+    if ((rc = make_plane_map(&dmap, D, g.H, g.W, g.pitch, bw, bh))) return rc;
+    for (int k = 0; k < 2; ++k) {
+        const float *in = bufs[k];
+        float *out = bufs[k ^ 1];
+        tm[k].d = dmap;
+        if ((rc = make_plane_map(&tm[k].v, in, g.H, g.W, g.pitch, bw, bh)) ||
+            (rc = make_plane_map(&tm[k].w, in + plane, g.H, g.W, g.pitch, bw, bh)) ||
+            (rc = make_plane_map(&tm[k].u, in + 2 * plane, g.H, g.W, g.pitch, bw, bh)) ||
+            (rc = make_plane_map(&tm[k].ov, out, g.H, g.W, g.pitch, ow, oh)) ||
+            (rc = make_plane_map(&tm[k].ow, out + plane, g.H, g.W, g.pitch, ow, oh)) ||
+            (rc = make_plane_map(&tm[k].ou, out + 2 * plane, g.H, g.W, g.pitch, ow, oh)))
+            return rc;
+    }
+    CUtensorMap tm_d;
+    if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
+    MapCache maps;
+    int cur = 0;
+    int64_t t = t0;
+    for (; t + depth <= t1; t += depth) {
+        StepArgs a;
+        fill_args(a, g, bufs[cur], D, m, st, n_stimuli, (float)dt, rdx, status, nullptr);
+        if (launch_tb(depth, tm[cur], a, t, s) != cudaSuccess) return FK_ERR_CUDA;
+        cur ^= 1;
+    }
+    for (; t < t1; ++t) {  // the remainder, one step per launch
+        if ((rc = step_once(g, bufs[cur], bufs[cur ^ 1], D, m, st, n_stimuli, t, (float)dt, rdx,
+                            false, tm_d, maps, status, s)))
+            return rc;
+        cur ^= 1;
+    }
+    if (cur == 1 && cudaMemcpyAsync(state, scratch, sizeof(float) * 3 * plane,
+                                    cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return FK_ERR_CUDA;
     return FK_OK;
 }
 

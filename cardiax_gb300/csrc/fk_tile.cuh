@@ -131,7 +131,7 @@ static __device__ __noinline__ float4 apply_stimuli(const StepArgs &a, unsigned 
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
         const int jj = j + m;
-        if (i >= a.H || jj >= a.W) continue;
+        if (i < 0 || i >= a.H || jj < 0 || jj >= a.W) continue;  // no stimulus outside the grid
         float acc = 0.0f;
         for (int s = 0; s < a.n_stim; ++s) {
             if (!((active >> s) & 1u)) continue;

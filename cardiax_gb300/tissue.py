@@ -180,11 +180,20 @@ class Tissue:
             self._flags = torch.zeros(n, dtype=torch.int32, device=self.device)
         return self._flags
 
-    def advance(self, t0: int, t1: int, schedule: str = "step") -> "Tissue":
+    def advance(self, t0: int, t1: int, schedule: str = "step", depth: int = 1) -> "Tissue":
         """Steps t0 .. t1-1 in place (cardiax/solve.py:92-100).  ``schedule="step"``: one launch
-        per step (chained with programmatic dependent launch); ``"flow"``: one cooperative
-        dataflow launch for the whole range.  Both give identical results."""
+        per step (chained with programmatic dependent launch), or with ``depth`` 2, 4 or 8 that
+        many steps per launch (temporal blocking); ``"flow"``: one cooperative dataflow launch
+        for the whole range.  All give identical results."""
         act = ctypes.byref(self.activation) if self.activation is not None else None
+        if schedule == "step" and depth != 1:
+            if act is not None:
+                raise ValueError("activation tracking runs one step per launch (depth=1)")
+            N.call("fk_forward_euler_tb", self.grid, self.state.data_ptr(),
+                   self.scratch.data_ptr(), self.D.data_ptr(), ctypes.byref(self.params),
+                   self.stim, self.n_stim, int(t0), int(t1), self.dt, self.dx, int(depth),
+                   stream_handle())
+            return self
         if schedule == "step":
             N.call("fk_forward_euler_tracked", self.grid, self.state.data_ptr(),
                    self.scratch.data_ptr(), self.D.data_ptr(), ctypes.byref(self.params),

@@ -142,6 +142,15 @@ int fk_forward_euler_tracked(fk_grid g, float *state, float *scratch, const floa
                              int64_t t0, int64_t t1, double dt, double dx,
                              const fk_activation *act, void *stream);
 
+/* Temporal blocking (no reference counterpart; same results bit for bit): fk_forward_euler with
+ * `depth` steps (1, 2, 4 or 8) per launch.  Each tile is loaded once with a 4*depth-cell halo,
+ * advanced `depth` times in shared memory (recomputing the halo ring) and stored once; the last
+ * (t1 - t0) mod depth steps, and grids whose last tile row or column is one cell wide (H % 32 or
+ * W % 64 == 1; H % 16 or W % 16 == 1 at depth 8), run one step per launch. */
+int fk_forward_euler_tb(fk_grid g, float *state, float *scratch, const float *D,
+                        const fk_params *p, const fk_stimulus *stimuli, int n_stimuli, int64_t t0,
+                        int64_t t1, double dt, double dx, int depth, void *stream);
+
 /* Dataflow stepping: fk_forward_euler_tracked and fk_forward in one cooperative launch per call
  * instead of one launch per step (no reference counterpart; same results bit for bit).  Tile T of
  * step t starts as soon as T and its eight neighbours have finished step t-1, tracked in
