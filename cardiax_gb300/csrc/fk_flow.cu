@@ -7,16 +7,19 @@
 // head and the launch gap, prologue and pipeline drain of per-step launches disappear.
 //
 // Work split: the (step, tile) items are numbered i = k * ntiles + T and CTA c of G takes items
-// c, c+G, c+2G, ... in order, so every CTA gets the same number of tiles (to within one) over
-// the whole launch.  Warp 0 of a CTA publishes flags[T] = k+1 once the TMA stores of item
-// (k, T) have completed, one tile late so that it never waits for them: at the hook between the
-// two passes of local item x it publishes item x-2 (cp.async.bulk.wait_group 1 leaves only the
-// stores of item x-1 pending).  The loads of a later item are issued once the flags of its
-// neighbourhood (relaxed loads made at the top of the item) cover the previous step; items of
-// this CTA are judged from its own progress.  One fence.acq_rel.gpu per tile serves both as the
-// release of the published flag and the acquire of the flags read.  A prefetch that is not
-// ready is retried at the next tile; an item whose loads were never issued publishes everything
-// pending, waits for its flags (bounded), then loads.
+// c, c+G, c+2G, ... in order (every CTA gets the same number of tiles to within one over the
+// launch); a CTA advances its (k, T) position incrementally, without divisions.
+//
+// Roles inside a CTA.  The last warp's lane 0 (the "store thread") issues the TMA stores of
+// every item and, at the top of item x, waits for the stores of items <= x-2 (bulk wait_group 1,
+// normally already done) and records that in shared memory.  Warp 0 then publishes those items
+// (flags[T] = k+1) at its hook between the two passes, reads the flags of the next item to
+// prefetch (relaxed loads made at the top of the item) and issues its TMA loads when its
+// neighbourhood is ready; items of this CTA are judged from its own progress.  One
+// fence.acq_rel.gpu in warp 0 per tile is both the release of the published flags and the
+// acquire of the flags read; warp 0 has no bulk stores in flight, so the fence does not wait
+// for them.  A prefetch that is not ready is retried at the next tile; an item whose loads were
+// never issued publishes everything completed, waits for its flags (bounded), then loads.
 //
 // Hazards covered by the flags: step k of tile T reads buffer (k-1)&1 around T (its own cells
 // and a 4-cell halo inside the neighbours), written by step k-1 of those tiles; it overwrites
@@ -38,41 +41,57 @@ namespace {
 
 constexpr uint64_t kFlagWaitNs = 1000000000ull;   // one dependency wait
 constexpr uint64_t kDrainWaitNs = 100000000ull;   // one in-flight load on the error path
+constexpr int kStoreThread = NT - 32;             // lane 0 of the last warp
 
 __device__ __forceinline__ void bulk_wait_all_but_one() {
     asm volatile("cp.async.bulk.wait_group 1;" ::: "memory");
 }
 
+// Position (step k, tile T) of an item; the next item of the CTA is G tiles further (G <= the
+// tile count, so at most one wrap into the next step).
+struct Pos {
+    int k, T;
+};
 struct Plan {
-    int ntx, nty, ntiles, G, c;
-    int64_t total;  // items of this CTA
-    __device__ __forceinline__ int64_t global_of(int64_t x) const { return c + x * G; }
-    __device__ __forceinline__ int step_of(int64_t x) const { return (int)(global_of(x) / ntiles); }
-    __device__ __forceinline__ int tile_of(int64_t x) const { return (int)(global_of(x) % ntiles); }
+    int ntx, nty, ntiles, G, c, r;  // r = ntiles mod G
+    int64_t total;                  // items of this CTA
+    __device__ __forceinline__ void next(Pos &p) const {
+        p.T += G;
+        if (p.T >= ntiles) {
+            p.T -= ntiles;
+            ++p.k;
+        }
+    }
+    __device__ __forceinline__ Pos ahead(Pos p, int n) const {
+        for (int i = 0; i < n; ++i) next(p);
+        return p;
+    }
 };
 
-// Dependency of local item x on neighbour `lane` (0..8, row-major 3x3 around its tile).
+// Dependency of the item at position p (local index x) on neighbour `lane` (0..8, row-major
+// 3x3 around its tile).
 struct Dep {
     int kind;         // 0: none, 1: an item of this CTA, 2: an item of another CTA
     int need;         // kind 2: flags[tile] must reach this
     int64_t own;      // kind 1: the local item that must have been published
     const int *flag;  // kind 2
 };
-__device__ __forceinline__ Dep dep_of(const Plan &P, const int *flags, int64_t x, int lane) {
+__device__ __forceinline__ Dep dep_of(const Plan &P, const int *flags, Pos p, int64_t x,
+                                      int lane) {
     Dep d{0, 0, 0, nullptr};
-    const int64_t i = P.global_of(x);
-    const int k = (int)(i / P.ntiles), T = (int)(i % P.ntiles);
-    if (k == 0 || lane >= 9) return d;
-    const int ti = T / P.ntx + lane / 3 - 1, tj = T % P.ntx + lane % 3 - 1;
+    if (p.k == 0 || lane >= 9) return d;
+    const int ti = p.T / P.ntx + lane / 3 - 1, tj = p.T % P.ntx + lane % 3 - 1;
     if (ti < 0 || ti >= P.nty || tj < 0 || tj >= P.ntx) return d;
     const int tn = ti * P.ntx + tj;
-    const int64_t in = (int64_t)(k - 1) * P.ntiles + tn;  // global number of the dependency
-    if (in % P.G == P.c) {
+    // global number of the dependency: i(p) - ntiles + (tn - T); it is this CTA's iff that
+    // difference is a multiple of G, and then it lies (ntiles - dT) / G items back
+    const int dT = tn - p.T;
+    if ((dT - P.r) % P.G == 0) {
         d.kind = 1;
-        d.own = in / P.G;
+        d.own = x - (P.ntiles - dT) / P.G;
     } else {
         d.kind = 2;
-        d.need = k;
+        d.need = p.k;
         d.flag = flags + tn;
     }
     return d;
@@ -93,7 +112,8 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
     io.ou = io.ow + TX * TY;
     uint64_t *bar = reinterpret_cast<uint64_t *>(io.ou + TX * TY);
     StepArgs *sa = reinterpret_cast<StepArgs *>(bar + NSTAGE);  // [3]: src, buffer 0, buffer 1
-    __shared__ long long s_issued;  // local items whose loads have been issued
+    __shared__ long long s_issued;  // local items whose loads have been issued (warp 0)
+    __shared__ long long s_stored;  // local items whose stores have completed (store thread)
 
     const int tid = threadIdx.x, lane = tid & 31;
     const StepArgs &a0 = fa.in[0];
@@ -103,6 +123,7 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
     P.ntiles = P.ntx * P.nty;
     P.G = gridDim.x;
     P.c = blockIdx.x;
+    P.r = P.ntiles % P.G;
     const int64_t n_items = (int64_t)P.ntiles * fa.nsteps;
     P.total = (n_items - P.c + P.G - 1) / P.G;
     int *flags = fa.flags;
@@ -114,48 +135,53 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
         for (int k = 0; k < NSTAGE; ++k) mbar_init(&bar[k], 1);
         fence_barrier_init();
         s_issued = 0;
+        s_stored = 0;
     }
     __syncthreads();
 
     auto in_sel = [](int k) { return k == 0 ? 0 : 1 + ((k - 1) & 1); };
-    auto issue = [&](int64_t x) {  // lane 0 of warp 0
-        const int k = P.step_of(x), T = P.tile_of(x);
-        const int st = (int)(x % NSTAGE);
+    auto issue = [&](Pos p, int stage) {  // lane 0 of warp 0
         fence_proxy_async_global();  // the flags read before are ordered before the TMA reads
-        issue_tile(&fm.uin[in_sel(k)], &fm.d, stage_at(smem, st), &bar[st], (T / P.ntx) * TY,
-                   (T % P.ntx) * TX);
+        issue_tile(&fm.uin[in_sel(p.k)], &fm.d, stage_at(smem, stage), &bar[stage],
+                   (p.T / P.ntx) * TY, (p.T % P.ntx) * TX);
     };
-    // Warp 0.  Own items < published have their flags written.  publish(n) writes the flags of
-    // items published .. n-1: their stores must have completed (bulk wait by lane 0 + proxy
-    // fence) and a fence.acq_rel.gpu must separate them from the flag stores.
+    // Warp 0: own items < published have their flags written; publish(n) writes the flags of
+    // items published .. n-1 (their stores have completed; the caller has fenced).
     int64_t published = 0;
+    Pos pub_pos{0, P.c};
     auto publish = [&](int64_t n) {
-        if (lane == 0)
-            for (int64_t y = published; y < n; ++y)
-                st_relaxed_gpu(flags + P.tile_of(y), P.step_of(y) + 1);
-        if (n > published) published = n;
+        for (; published < n; ++published) {
+            if (lane == 0) st_relaxed_gpu(flags + pub_pos.T, pub_pos.k + 1);
+            P.next(pub_pos);
+        }
+    };
+    auto stores_completed = [&](int64_t upto) {  // store thread
+        fence_proxy_async_global();
+        s_stored = upto;
     };
 
     bool failed = false;
     int64_t x = 0;
+    Pos cur{0, P.c};
+    int stage = 0;
+    uint32_t phase = 0;
     for (; x < P.total; ++x) {
-        const int k = P.step_of(x), T = P.tile_of(x);
+        const int k = cur.k, T = cur.T;
         const int i0 = (T / P.ntx) * TY, j0 = (T % P.ntx) * TX;
         const StepArgs &a = sa[in_sel(k)];
         int64_t issued = *(volatile long long *)&s_issued;  // uniform: written before a barrier
 
         if (issued == x) {  // nothing prefetched: publish, wait for this item's inputs, load
+            if (tid == kStoreThread) {
+                bulk_wait_all();
+                stores_completed(x);
+            }
+            __syncthreads();
             bool ok = true;
             if (tid < 32) {
-                if (lane == 0) {
-                    bulk_wait_all();
-                    fence_proxy_async_global();
-                }
-                __syncwarp();
                 fence_acq_rel_gpu();
-                publish(x);
-                __syncwarp();
-                const Dep d = dep_of(P, flags, x, lane);
+                publish(*(volatile long long *)&s_stored);
+                const Dep d = dep_of(P, flags, cur, x, lane);
                 if (d.kind == 2 && ld_relaxed_gpu(d.flag) < d.need) {
                     const uint64_t t_start = global_timer_ns();
                     while (ld_relaxed_gpu(d.flag) < d.need) {
@@ -171,7 +197,7 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
                 if (ok) {
                     fence_acq_rel_gpu();
                     __syncwarp();
-                    if (lane == 0) issue(x);
+                    if (lane == 0) issue(cur, stage);
                 }
             }
             // s_issued changes only after a barrier that every thread passes after reading it
@@ -181,19 +207,25 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
             }
             if (tid == 0) s_issued = x + 1;
             issued = x + 1;
+        } else if (tid == kStoreThread && x >= 2) {
+            bulk_wait_all_but_one();  // the stores of items <= x-2 have completed
+            stores_completed(x - 1);
         }
 
         // warp 0: read the flags of the next item to prefetch (judged after pass 1)
-        const int64_t cand = (issued < P.total && issued < x + NSTAGE) ? issued : -1;
+        const int ahead = (int)(issued - x);  // 1 or 2
+        const bool have_cand = issued < P.total && ahead < NSTAGE;
+        Pos cpos{0, 0};
         Dep cd{0, 0, 0, nullptr};
         int cflag = 0;
-        if (tid < 32 && cand >= 0) {
-            cd = dep_of(P, flags, cand, lane);
+        if (tid < 32 && have_cand) {
+            cpos = P.ahead(cur, ahead);
+            cd = dep_of(P, flags, cpos, issued, lane);
             if (cd.kind == 2) cflag = ld_relaxed_gpu(cd.flag);
         }
 
         load_vw(a, i0, j0, io);
-        const bool landed = mbar_wait_bounded(&bar[x % NSTAGE], (uint32_t)((x / NSTAGE) & 1));
+        const bool landed = mbar_wait_bounded(&bar[stage], phase);
         if (__syncthreads_or(!landed)) {
             failed = true;
             break;
@@ -203,43 +235,47 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
         for (int s = 0; s < a.n_stim; ++s)
             if (stim_active(a.stim[s], t)) active |= 1u << s;
 
-        auto after_pass1 = [&] {  // warp 0, between the passes
-            if (lane == 0) {
-                bulk_wait_all_but_one();  // stores of items <= x-2 have completed
-                fence_proxy_async_global();
-            }
-            __syncwarp();
-            // own items published after this hook: < x-1
-            const bool ready = cand >= 0 &&
-                               (cd.kind == 0 || (cd.kind == 1 && cd.own < x - 1) ||
-                                (cd.kind == 2 && cflag >= cd.need));
-            const bool go = __all_sync(0xffffffffu, ready);
-            if (go || published < x - 1) {
-                fence_acq_rel_gpu();  // release for the flags below, acquire for cflag
-                publish(x - 1);
-            }
-            if (go) {
-                __syncwarp();
-                if (lane == 0) {
-                    issue(cand);
-                    s_issued = cand + 1;
+        auto after_pass1 = [&] {  // between the passes
+            if (tid < 32) {
+                const int64_t done = *(volatile long long *)&s_stored;
+                const bool ready = have_cand &&
+                                   (cd.kind == 0 || (cd.kind == 1 && cd.own < done) ||
+                                    (cd.kind == 2 && cflag >= cd.need));
+                const bool go = __all_sync(0xffffffffu, ready);
+                if (go || published < done) {
+                    fence_acq_rel_gpu();  // release for the flags below, acquire for cflag
+                    publish(done);
+                }
+                if (go) {
+                    __syncwarp();
+                    if (lane == 0) {
+                        int cs = stage + ahead;
+                        if (cs >= NSTAGE) cs -= NSTAGE;
+                        issue(cpos, cs);
+                        s_issued = issued + 1;
+                    }
                 }
             }
-            if (lane == 0) bulk_wait_read();  // the output tiles are free for pass 2
+            if (tid == kStoreThread) bulk_wait_read();  // the output tiles are free for pass 2
         };
-        process_tile<false, ACT>(a, t, stage_at(smem, (int)(x % NSTAGE)), sux, suy, io, active,
-                                 i0, j0, after_pass1);
+        process_tile<false, ACT>(a, t, stage_at(smem, stage), sux, suy, io, active, i0, j0,
+                                 after_pass1);
         const int o = k & 1;
-        store_tile(&fm.ov[o], &fm.ow[o], &fm.ou[o], io, i0, j0);
+        store_tile(&fm.ov[o], &fm.ow[o], &fm.ou[o], io, i0, j0, kStoreThread);
+        P.next(cur);
+        if (++stage == NSTAGE) {
+            stage = 0;
+            phase ^= 1u;
+        }
     }
 
     if (!failed) {
+        if (tid == kStoreThread) {
+            bulk_wait_all();
+            stores_completed(x);
+        }
+        __syncthreads();
         if (tid < 32) {
-            if (lane == 0) {
-                bulk_wait_all();
-                fence_proxy_async_global();
-            }
-            __syncwarp();
             fence_acq_rel_gpu();
             publish(x);
         }
@@ -250,10 +286,17 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
         st_relaxed_gpu(abort_word, 1);
         atomicOr(a0.status, kStatusTimeout);
         const int64_t issued = *(volatile long long *)&s_issued;
-        for (int64_t y = x; y < issued; ++y)
-            mbar_wait_bounded(&bar[y % NSTAGE], (uint32_t)((y / NSTAGE) & 1), kDrainWaitNs);
-        bulk_wait_all();
+        int st = stage;
+        uint32_t ph = phase;
+        for (int64_t y = x; y < issued; ++y) {
+            mbar_wait_bounded(&bar[st], ph, kDrainWaitNs);
+            if (++st == NSTAGE) {
+                st = 0;
+                ph ^= 1u;
+            }
+        }
     }
+    if (tid == kStoreThread) bulk_wait_all();
 }
 
 cudaError_t launch_flow(const FlowMaps &maps, const FlowArgs &a, bool act, cudaStream_t stream) {

@@ -108,17 +108,22 @@ struct Reaction {
 __device__ __forceinline__ Reaction reaction(float u, float v, float w, const Model &m) {
     const bool p = u >= m.V_c;
     const bool q = u >= m.V_v;
+    // both sides of every gate are evaluated, then selected (no branches)
     // j_fi = -v p (u - V_c)(1 - u) / tau_d  (zero when the gate is closed)
-    float j_fi = p ? ((-v * (u - m.V_c)) * (1.0f - u)) * m.r_tau_d : 0.0f;
+    const float jfi_on = ((-v * (u - m.V_c)) * (1.0f - u)) * m.r_tau_d;
+    const float j_fi = p ? jfi_on : 0.0f;
     // j_so = u (1 - p) / tau_0 + p / tau_r
-    float j_so = p ? m.inv_tau_r : u * m.r_tau_0;
+    const float jso_off = u * m.r_tau_0;
+    const float j_so = p ? m.inv_tau_r : jso_off;
     // j_si = -w (1 + tanh(k (u - V_csi))) / (2 tau_si)
-    float j_si = -(w * one_plus_tanh(m.k * (u - m.V_csi))) * m.r_2tau_si;
+    const float j_si = -(w * one_plus_tanh(m.k * (u - m.V_csi))) * m.r_2tau_si;
     Reaction r;
     r.j_ion = -((j_fi + j_so) + j_si) * m.r_Cm;
     const float r_tvm = q ? m.r_tau_v2m : m.r_tau_v1m;
-    r.dv = p ? -(v * m.r_tau_vp) : (1.0f - v) * r_tvm;
-    r.dw = p ? -(w * m.r_tau_wp) : (1.0f - w) * m.r_tau_wm;
+    const float dv_on = -(v * m.r_tau_vp), dv_off = (1.0f - v) * r_tvm;
+    const float dw_on = -(w * m.r_tau_wp), dw_off = (1.0f - w) * m.r_tau_wm;
+    r.dv = p ? dv_on : dv_off;
+    r.dw = p ? dw_on : dw_off;
     return r;
 }
 
@@ -127,5 +132,7 @@ __device__ __forceinline__ float diffusion(float d, float dx_, float dy_, float 
                                            float uxx, float uyy) {
     return fmaf(dy_, uy, fmaf(dx_, ux, d * (uxx + uyy)));
 }
+
+
 
 }  // namespace fk

@@ -341,7 +341,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
         }
         suy[r * SW + c] = o * rdx;
     }
-    if (tid < 32) after_pass1();  // warp 0: e.g. free the output tiles, start further loads
+    after_pass1();  // every thread (the hook picks its warps): free the output tiles, start loads
     __syncthreads();
 
     // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
@@ -491,10 +491,10 @@ __device__ __forceinline__ void process_tile(const StepArgs &a, float t, const S
 // Writes the output tiles with TMA stores (after all threads have written them).
 __device__ __forceinline__ void store_tile(const CUtensorMap *ov, const CUtensorMap *ow,
                                            const CUtensorMap *ou, const TileIO &io, int i0,
-                                           int j0) {
+                                           int j0, int issuer = 0) {
     fence_async_smem();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == issuer) {
         tma_store_2d(ov, io.ov, j0, i0);
         tma_store_2d(ow, io.ow, j0, i0);
         tma_store_2d(ou, io.ou, j0, i0);
