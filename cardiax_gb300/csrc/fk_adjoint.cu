@@ -29,8 +29,6 @@ namespace fk {
 
 namespace {
 
-constexpr int AB = 16;  // block edge (AB x AB threads)
-
 __device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
 
 // Coefficient of P[m] in row k of G on a padded line of length L (cardiax/solve.py:225-254).
@@ -141,156 +139,280 @@ __device__ __forceinline__ float fwd_d2(F at, int i, int N, float rdx) {
     return s * rdx;
 }
 
-__global__ void __launch_bounds__(AB *AB)
-    fk_adjoint_kernel(const __grid_constant__ AdjointArgs a) {
-    const int j = blockIdx.x * AB + threadIdx.x;
-    const int i = blockIdx.y * AB + threadIdx.y;
-    const int H = a.H, W = a.W, pitch = a.pitch;
-    const bool in = i < H && j < W;
-    const float dt = a.dt, rdx = a.rdx;
+// Pointwise part of the adjoint of one cell: cotangents through the gates and currents, and the
+// cell's contribution to dL/dtheta (added into gth).  Returns mu = dt lam'_u.
+__device__ __forceinline__ float adjoint_pointwise(const AdjointArgs &a, int i, int j, int64_t off,
+                                                  float &olv, float &olw, float &olu,
+                                                  float *gth) {
     const Model &m = a.m;
+    const float dt = a.dt;
+    const float u = __ldg(a.u + off), v = __ldg(a.v + off), w = __ldg(a.w + off);
+    const float lu = __ldg(a.lu + off), lv = __ldg(a.lv + off), lw = __ldg(a.lw + off);
+    const float mu = dt * lu;
+    bool stim = false;
+    for (int s = 0; s < a.n_stim; ++s) {
+        if (!stim_active(a.stim[s], a.t)) continue;
+        const Stim &st = a.stim[s];
+        const float fv = st.field ? __ldg(st.field + off)
+                                  : ((i >= st.r0 && i < st.r1 && j >= st.c0 && j < st.c1)
+                                         ? st.amplitude : 0.0f);
+        if (fv != 0.0f) stim = true;
+    }
+    const bool p = u >= m.V_c, q = u >= m.V_v;
+    const float S = one_plus_tanh(m.k * (u - m.V_csi));  // 1 + tanh
+    const float sech2 = S * (2.0f - S);                  // 1 - tanh^2
+    const float r_tvm = q ? m.r_tau_v2m : m.r_tau_v1m;
+    const float dvdv = 1.0f + dt * (p ? -m.r_tau_vp : -r_tvm);
+    const float dwdw = 1.0f + dt * (p ? -m.r_tau_wp : -m.r_tau_wm);
+    float dJdu = 0.f, dJdv = 0.f, dJdw = 0.f;
+    if (!stim) {
+        const float dfi = p ? -v * (1.0f + m.V_c - 2.0f * u) * m.r_tau_d : 0.0f;
+        const float dso = p ? 0.0f : m.r_tau_0;
+        const float dsi = -w * m.k * sech2 * m.r_2tau_si;
+        dJdu = -(dfi + dso + dsi) * m.r_Cm;
+        dJdv = p ? (u - m.V_c) * (1.0f - u) * m.r_tau_d * m.r_Cm : 0.0f;
+        dJdw = S * m.r_2tau_si * m.r_Cm;
+    }
+    olv = lv * dvdv + mu * dJdv;
+    olw = lw * dwdw + mu * dJdw;
+    olu = lu * (1.0f + dt * dJdu);
+
+    // parameter gradients (cardiax/params.py fields 0..12)
+    const float pv = p ? 1.0f : 0.0f, qv = q ? 1.0f : 0.0f;
+    gth[0] += lv * dt * pv * v * m.r_tau_vp * m.r_tau_vp;                           // tau_v_plus
+    gth[1] += -lv * dt * (1.f - pv) * (1.f - v) * (1.f - qv) * m.r_tau_v1m * m.r_tau_v1m;
+    gth[2] += -lv * dt * (1.f - pv) * (1.f - v) * qv * m.r_tau_v2m * m.r_tau_v2m;
+    gth[3] += lw * dt * pv * w * m.r_tau_wp * m.r_tau_wp;                           // tau_w_plus
+    gth[4] += -lw * dt * (1.f - pv) * (1.f - w) * m.r_tau_wm * m.r_tau_wm;           // tau_w_minus
+    if (!stim) {
+        gth[5] += mu * (-v * pv * (u - m.V_c) * (1.f - u) * m.r_tau_d * m.r_tau_d) * m.r_Cm;
+        gth[6] += mu * (u * (1.f - pv) * m.r_tau_0 * m.r_tau_0) * m.r_Cm;            // tau_0
+        gth[7] += mu * (pv * m.inv_tau_r * m.inv_tau_r) * m.r_Cm;                    // tau_r
+        gth[8] += mu * (-w * S * 2.0f * m.r_2tau_si * m.r_2tau_si) * m.r_Cm;         // tau_si
+        gth[9] += mu * (w * sech2 * (u - m.V_csi) * m.r_2tau_si) * m.r_Cm;           // k
+        gth[10] += mu * (-w * m.k * sech2 * m.r_2tau_si) * m.r_Cm;                   // V_csi
+        gth[11] += mu * (-v * pv * (1.f - u) * m.r_tau_d) * m.r_Cm;                  // V_c
+    }
+    // gth[12] (V_v) enters only through a Heaviside gate: zero
+    return mu;
+}
+
+// One axis of the diffusion transpose at a cell within ADJ_BAND of an edge along that axis:
+// the explicit transposed rows (one-sided rows and the fold of the edge pad), reading global
+// memory.  AXIS 0: along rows (x), 1: along columns (y).
+struct AxisTerms {
+    float AT, BT, d2, g;  // A^T(D mu), B^T((B D) mu), u_xx (or u_yy), B^T(mu u_x) (or y)
+};
+template <int AXIS>
+__device__ AxisTerms axis_explicit(const AdjointArgs &a, int i, int j) {
+    const int H = a.H, W = a.W, pitch = a.pitch;
+    const float dt = a.dt, rdx = a.rdx;
+    const float *D = a.D, *U = a.u, *LU = a.lu;
+    auto at = [&](const float *p, int r, int c) {
+        return __ldg(p + (int64_t)clampi(r, 0, H - 1) * pitch + clampi(c, 0, W - 1));
+    };
+    AxisTerms t;
+    if (AXIS == 0) {
+        auto Dx_at = [&](int r) { return fwd_d1([&](int x) { return at(D, x, j); }, r, H) * rdx; };
+        auto Ux_at = [&](int r) { return fwd_d1([&](int x) { return at(U, x, j); }, r, H) * rdx; };
+        auto Mcol = [&](int r) { return dt * __ldg(LU + (int64_t)r * pitch + j); };
+        const auto qx = make_line([&](int r) { return at(D, r, j) * Mcol(r); }, H);
+        const auto bx = make_line([&](int r) { return Dx_at(r) * Mcol(r); }, H);
+        const auto gxl = make_line([&](int r) { return Mcol(r) * Ux_at(r); }, H);
+        t.AT = qx.AT(i) * (rdx * rdx);
+        t.BT = bx.BT(i) * rdx;
+        t.d2 = fwd_d2([&](int r) { return at(U, r, j); }, i, H, rdx);
+        t.g = gxl.BT(i) * rdx;
+    } else {
+        auto Dy_at = [&](int c) { return fwd_d1([&](int y) { return at(D, i, y); }, c, W) * rdx; };
+        auto Uy_at = [&](int c) { return fwd_d1([&](int y) { return at(U, i, y); }, c, W) * rdx; };
+        auto Mrow = [&](int c) { return dt * __ldg(LU + (int64_t)i * pitch + c); };
+        const auto qy = make_line([&](int c) { return at(D, i, c) * Mrow(c); }, W);
+        const auto by = make_line([&](int c) { return Dy_at(c) * Mrow(c); }, W);
+        const auto gyl = make_line([&](int c) { return Mrow(c) * Uy_at(c); }, W);
+        t.AT = qy.AT(j) * (rdx * rdx);
+        t.BT = by.BT(j) * rdx;
+        t.d2 = fwd_d2([&](int c) { return at(U, i, c); }, j, W, rdx);
+        t.g = gyl.BT(j) * rdx;
+    }
+    return t;
+}
+
+// Corner blocks (cells 0..9 of a line) of the line operators B' = C G E and A' = C G G E
+// (E the edge pad, G the padded-line derivative of cardiax/solve.py:225-254, C the crop), built
+// in double at compile time on a line of 40 cells.  Both operators are banded (|r - i| <= 4),
+// so the corner is the same for every line of at least 18 cells, and the far corner is the
+// reflection: A'[N-1-r][N-1-i] = A'[r][i], B'[N-1-r][N-1-i] = -B'[r][i].
+struct EdgeTables {
+    float A[10][10], B[10][10];
+};
+constexpr double gd(int k, int m, int L) {  // G[k][m] on a padded line of length L
+    if (k < 2) {
+        const int o = m - k;
+        return o == 0 ? -11.0 / 6.0 : o == 1 ? 3.0 : o == 2 ? -1.5 : o == 3 ? 1.0 / 3.0 : 0.0;
+    }
+    if (k > L - 3) {
+        const int o = m - (k - 3);
+        return o == 0 ? -1.0 / 3.0 : o == 1 ? 1.5 : o == 2 ? -3.0 : o == 3 ? 11.0 / 6.0 : 0.0;
+    }
+    const int o = m - k;
+    return o == -2 ? 1.0 / 12.0 : o == -1 ? -2.0 / 3.0 : o == 1 ? 2.0 / 3.0 : o == 2 ? -1.0 / 12.0 : 0.0;
+}
+constexpr double ge(int m, int i, int N) {  // (G E)[m][i]
+    const int L = N + 2;
+    return gd(m, i + 1, L) + (i == 0 ? gd(m, 0, L) : 0.0) + (i == N - 1 ? gd(m, L - 1, L) : 0.0);
+}
+constexpr EdgeTables make_edge_tables() {
+    constexpr int N = 40, L = N + 2;
+    EdgeTables t{};
+    for (int r = 0; r < 10; ++r)
+        for (int i = 0; i < 10; ++i) {
+            double a = 0.0;
+            for (int m = 0; m < L; ++m) a += gd(r + 1, m, L) * ge(m, i, N);
+            t.A[r][i] = (float)a;
+            t.B[r][i] = (float)ge(r + 1, i, N);
+        }
+    return t;
+}
+constexpr EdgeTables kEdgeHost = make_edge_tables();
+__constant__ EdgeTables kEdge = kEdgeHost;
+constexpr int kEdgeMinLine = 20;  // shorter lines use the explicit rows of axis_explicit
+
+// One axis of the diffusion transpose at a cell within ADJ_BAND of an end of its line, from
+// the corner tables: 10 cells of the line nearest that end.
+template <int AXIS>
+__device__ AxisTerms axis_edge(const AdjointArgs &a, int i, int j) {
+    const int N = AXIS == 0 ? a.H : a.W;
+    const int pos = AXIS == 0 ? i : j;
+    if (N < kEdgeMinLine) return axis_explicit<AXIS>(a, i, j);
+    const int pitch = a.pitch;
+    const float dt = a.dt, rdx = a.rdx;
+    const bool near0 = pos < ADJ_BAND;
+    const int pp = near0 ? pos : N - 1 - pos;  // distance from the near end
+    auto at = [&](const float *f, int q) {
+        q = clampi(q, 0, N - 1);
+        return __ldg(f + (AXIS == 0 ? (int64_t)q * pitch + j : (int64_t)i * pitch + q));
+    };
+    float AT = 0.f, BT = 0.f, d2 = 0.f, g = 0.f;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const int q = near0 ? r : N - 1 - r;
+        const float mu = dt * at(a.lu, q);
+        const float dq = fwd_d1([&](int x) { return at(a.D, x); }, q, N) * rdx;
+        const float uq = fwd_d1([&](int x) { return at(a.u, x); }, q, N) * rdx;
+        AT = fmaf(kEdge.A[r][pp], at(a.D, q) * mu, AT);
+        BT = fmaf(kEdge.B[r][pp], dq * mu, BT);
+        d2 = fmaf(kEdge.A[pp][r], at(a.u, q), d2);
+        g = fmaf(kEdge.B[r][pp], mu * uq, g);
+    }
+    const float sgn = near0 ? 1.0f : -1.0f;
+    AxisTerms t;
+    t.AT = AT * (rdx * rdx);
+    t.BT = sgn * BT * rdx;
+    t.d2 = d2 * (rdx * rdx);
+    t.g = sgn * g * rdx;
+    return t;
+}
+
+// Tile geometry: ATY x ATX cells per block, a 4-cell halo of u, D and mu in shared memory.
+constexpr int ATX = 32, ATY = 16, AHALO = 4;
+constexpr int ASW = ATX + 2 * AHALO, ASH = ATY + 2 * AHALO;
+constexpr int ANT = 256;
+constexpr int AXW = ATX;      // row width of the x-derivative planes (tile rows -2 .. ATY+1)
+constexpr int AYW = ATX + 4;  // row width of the y-derivative planes (tile columns -2 .. ATX+1)
+
+// Interior cells (at least ADJ_BAND from both ends of an axis) use G^T = -G on central rows:
+// along x, A_x^T(D mu) = G G (D mu) / dx^2, B_x^T(D_x mu) = -G (D_x mu) / dx and
+// B_x^T(mu u_x) = -G (mu u_x) / dx, from first derivatives staged in shared memory.
+__global__ void __launch_bounds__(ANT) fk_adjoint_kernel(const __grid_constant__ AdjointArgs a) {
+    __shared__ float su[ASH * ASW], sd[ASH * ASW], sm[ASH * ASW];  // u, D, mu = dt lam'_u
+    __shared__ float sux[(ATY + 4) * AXW], sqx[(ATY + 4) * AXW], sbx[(ATY + 4) * AXW];
+    __shared__ float suy[ATY * AYW], sqy[ATY * AYW], sby[ATY * AYW];
+    __shared__ float red[kAdjParams][ANT / 32];
+    const int tid = threadIdx.x;
+    const int H = a.H, W = a.W, pitch = a.pitch;
+    const float dt = a.dt, rdx = a.rdx;
+    const int i0 = blockIdx.y * ATY, j0 = blockIdx.x * ATX;
+
+    // u, D, mu with a 4-cell halo; out-of-grid positions hold clamped copies, read only by
+    // cells that take the explicit path along that axis
+    for (int k = tid; k < ASH * ASW; k += ANT) {
+        const int r = k / ASW, c = k % ASW;
+        const int64_t g = (int64_t)clampi(i0 - AHALO + r, 0, H - 1) * pitch +
+                          clampi(j0 - AHALO + c, 0, W - 1);
+        su[k] = __ldg(a.u + g);
+        sd[k] = __ldg(a.D + g);
+        sm[k] = dt * __ldg(a.lu + g);
+    }
+    __syncthreads();
+    // x: u_x, G_x(D mu), D_x mu on tile rows -2 .. ATY+1
+    for (int k = tid; k < (ATY + 4) * AXW; k += ANT) {
+        const int r = k / AXW, c = k % AXW;
+        const int b = (r - 2 + AHALO) * ASW + c + AHALO;
+        auto U = [&](int d) { return su[b + d * ASW]; };
+        auto Dd = [&](int d) { return sd[b + d * ASW]; };
+        auto M = [&](int d) { return sm[b + d * ASW]; };
+        sux[k] = g_central(U(-2), U(-1), U(1), U(2)) * rdx;
+        sqx[k] = g_central(Dd(-2) * M(-2), Dd(-1) * M(-1), Dd(1) * M(1), Dd(2) * M(2)) * rdx;
+        sbx[k] = (g_central(Dd(-2), Dd(-1), Dd(1), Dd(2)) * rdx) * M(0);
+    }
+    // y: the same on tile columns -2 .. ATX+1
+    for (int k = tid; k < ATY * AYW; k += ANT) {
+        const int r = k / AYW, c = k % AYW;
+        const int b = (r + AHALO) * ASW + c - 2 + AHALO;
+        auto U = [&](int d) { return su[b + d]; };
+        auto Dd = [&](int d) { return sd[b + d]; };
+        auto M = [&](int d) { return sm[b + d]; };
+        suy[k] = g_central(U(-2), U(-1), U(1), U(2)) * rdx;
+        sqy[k] = g_central(Dd(-2) * M(-2), Dd(-1) * M(-1), Dd(1) * M(1), Dd(2) * M(2)) * rdx;
+        sby[k] = (g_central(Dd(-2), Dd(-1), Dd(1), Dd(2)) * rdx) * M(0);
+    }
+    __syncthreads();
 
     float gth[kAdjParams];
 #pragma unroll
     for (int k = 0; k < kAdjParams; ++k) gth[k] = 0.0f;
-
-    if (in) {
-        auto at = [&](const float *p, int r, int c) {
-            return __ldg(p + (int64_t)clampi(r, 0, H - 1) * pitch + clampi(c, 0, W - 1));
-        };
+    for (int k = tid; k < ATY * ATX; k += ANT) {
+        const int r = k / ATX, c = k % ATX;
+        const int i = i0 + r, j = j0 + c;
+        if (i >= H || j >= W) continue;
         const int64_t off = (int64_t)i * pitch + j;
-        const float u = __ldg(a.u + off), v = __ldg(a.v + off), w = __ldg(a.w + off);
-        const float lu = __ldg(a.lu + off), lv = __ldg(a.lv + off), lw = __ldg(a.lw + off);
-        const float mu = dt * lu;
-
-        // ---- pointwise part -------------------------------------------------------------
-        bool stim = false;
-        for (int s = 0; s < a.n_stim; ++s) {
-            if (!stim_active(a.stim[s], a.t)) continue;
-            const Stim &st = a.stim[s];
-            const float fv = st.field ? __ldg(st.field + off)
-                                      : ((i >= st.r0 && i < st.r1 && j >= st.c0 && j < st.c1)
-                                             ? st.amplitude : 0.0f);
-            if (fv != 0.0f) stim = true;
-        }
-        const bool p = u >= m.V_c, q = u >= m.V_v;
-        const float S = one_plus_tanh(m.k * (u - m.V_csi));  // 1 + tanh
-        const float sech2 = S * (2.0f - S);                  // 1 - tanh^2
-        const float r_tvm = q ? m.r_tau_v2m : m.r_tau_v1m;
-        const float dvdv = 1.0f + dt * (p ? -m.r_tau_vp : -r_tvm);
-        const float dwdw = 1.0f + dt * (p ? -m.r_tau_wp : -m.r_tau_wm);
-        float dJdu = 0.f, dJdv = 0.f, dJdw = 0.f;
-        if (!stim) {
-            const float dfi = p ? -v * (1.0f + m.V_c - 2.0f * u) * m.r_tau_d : 0.0f;
-            const float dso = p ? 0.0f : m.r_tau_0;
-            const float dsi = -w * m.k * sech2 * m.r_2tau_si;
-            dJdu = -(dfi + dso + dsi) * m.r_Cm;
-            dJdv = p ? (u - m.V_c) * (1.0f - u) * m.r_tau_d * m.r_Cm : 0.0f;
-            dJdw = S * m.r_2tau_si * m.r_Cm;
-        }
-        float olv = lv * dvdv + mu * dJdv;
-        float olw = lw * dwdw + mu * dJdw;
-        float olu = lu * (1.0f + dt * dJdu);
-
-        // ---- parameter gradients (cardiax/params.py fields 0..12) ------------------------
-        const float pv = p ? 1.0f : 0.0f, qv = q ? 1.0f : 0.0f;
-        gth[0] = lv * dt * pv * v * m.r_tau_vp * m.r_tau_vp;                           // tau_v_plus
-        gth[1] = -lv * dt * (1.f - pv) * (1.f - v) * (1.f - qv) * m.r_tau_v1m * m.r_tau_v1m;
-        gth[2] = -lv * dt * (1.f - pv) * (1.f - v) * qv * m.r_tau_v2m * m.r_tau_v2m;
-        gth[3] = lw * dt * pv * w * m.r_tau_wp * m.r_tau_wp;                           // tau_w_plus
-        gth[4] = -lw * dt * (1.f - pv) * (1.f - w) * m.r_tau_wm * m.r_tau_wm;           // tau_w_minus
-        if (!stim) {
-            gth[5] = mu * (-v * pv * (u - m.V_c) * (1.f - u) * m.r_tau_d * m.r_tau_d) * m.r_Cm;
-            gth[6] = mu * (u * (1.f - pv) * m.r_tau_0 * m.r_tau_0) * m.r_Cm;            // tau_0
-            gth[7] = mu * (pv * m.inv_tau_r * m.inv_tau_r) * m.r_Cm;                    // tau_r
-            gth[8] = mu * (-w * S * 2.0f * m.r_2tau_si * m.r_2tau_si) * m.r_Cm;         // tau_si
-            gth[9] = mu * (w * sech2 * (u - m.V_csi) * m.r_2tau_si) * m.r_Cm;           // k
-            gth[10] = mu * (-w * m.k * sech2 * m.r_2tau_si) * m.r_Cm;                   // V_csi
-            gth[11] = mu * (-v * pv * (1.f - u) * m.r_tau_d) * m.r_Cm;                  // V_c
-        }
-        // gth[12] (V_v) enters only through a Heaviside gate: zero
-
-        // ---- diffusion transpose and dL/dD, axis by axis --------------------------------
-        // Along an axis, a cell at least ADJ_BAND from both ends uses the interior form
-        // (G^T = -G); otherwise the explicit transposed rows and the edge-pad fold.
-        const float *D = a.D, *U = a.u, *LU = a.lu;
-        auto Dat = [&](int r, int c) { return __ldg(D + (int64_t)r * pitch + c); };
-        auto Uat = [&](int r, int c) { return __ldg(U + (int64_t)r * pitch + c); };
-        auto Mat = [&](int r, int c) { return dt * __ldg(LU + (int64_t)r * pitch + c); };
-        float ATx, BTx, uxx, gx, ATy, BTy, uyy, gy;
+        float olv, olw, olu;
+        const float mu = adjoint_pointwise(a, i, j, off, olv, olw, olu, gth);
+        AxisTerms x, y;
         if (i >= ADJ_BAND && i < H - ADJ_BAND) {
-            auto Dx = [&](int r) {
-                return g_central(Dat(r - 2, j), Dat(r - 1, j), Dat(r + 1, j), Dat(r + 2, j)) * rdx;
-            };
-            auto Ux = [&](int r) {
-                return g_central(Uat(r - 2, j), Uat(r - 1, j), Uat(r + 1, j), Uat(r + 2, j)) * rdx;
-            };
-            auto Q1 = [&](int r) {  // G_x(D mu) at (r, j), scaled
-                return g_central(Dat(r - 2, j) * Mat(r - 2, j), Dat(r - 1, j) * Mat(r - 1, j),
-                                 Dat(r + 1, j) * Mat(r + 1, j), Dat(r + 2, j) * Mat(r + 2, j)) * rdx;
-            };
-            ATx = g_central(Q1(i - 2), Q1(i - 1), Q1(i + 1), Q1(i + 2)) * rdx;
-            BTx = -g_central(Dx(i - 2) * Mat(i - 2, j), Dx(i - 1) * Mat(i - 1, j),
-                             Dx(i + 1) * Mat(i + 1, j), Dx(i + 2) * Mat(i + 2, j)) * rdx;
-            const float ux_m2 = Ux(i - 2), ux_m1 = Ux(i - 1), ux_p1 = Ux(i + 1), ux_p2 = Ux(i + 2);
-            uxx = g_central(ux_m2, ux_m1, ux_p1, ux_p2) * rdx;
-            gx = -g_central(Mat(i - 2, j) * ux_m2, Mat(i - 1, j) * ux_m1, Mat(i + 1, j) * ux_p1,
-                            Mat(i + 2, j) * ux_p2) * rdx;
+            auto X = [&](const float *f, int d) { return f[(r + 2 + d) * AXW + c]; };
+            auto M = [&](int d) { return sm[(r + AHALO + d) * ASW + c + AHALO]; };
+            x.AT = g_central(X(sqx, -2), X(sqx, -1), X(sqx, 1), X(sqx, 2)) * rdx;
+            x.BT = -g_central(X(sbx, -2), X(sbx, -1), X(sbx, 1), X(sbx, 2)) * rdx;
+            x.d2 = g_central(X(sux, -2), X(sux, -1), X(sux, 1), X(sux, 2)) * rdx;
+            x.g = -g_central(M(-2) * X(sux, -2), M(-1) * X(sux, -1), M(1) * X(sux, 1),
+                             M(2) * X(sux, 2)) * rdx;
         } else {
-            auto Dx_at = [&](int r) { return fwd_d1([&](int x) { return at(D, x, j); }, r, H) * rdx; };
-            auto Ux_at = [&](int r) { return fwd_d1([&](int x) { return at(U, x, j); }, r, H) * rdx; };
-            auto Mcol = [&](int r) { return dt * __ldg(LU + (int64_t)r * pitch + j); };
-            const auto qx = make_line([&](int r) { return at(D, r, j) * Mcol(r); }, H);
-            const auto bx = make_line([&](int r) { return Dx_at(r) * Mcol(r); }, H);
-            const auto gxl = make_line([&](int r) { return Mcol(r) * Ux_at(r); }, H);
-            ATx = qx.AT(i) * (rdx * rdx);
-            BTx = bx.BT(i) * rdx;
-            uxx = fwd_d2([&](int r) { return at(U, r, j); }, i, H, rdx);
-            gx = gxl.BT(i) * rdx;
+            x = axis_edge<0>(a, i, j);
         }
         if (j >= ADJ_BAND && j < W - ADJ_BAND) {
-            auto Dy = [&](int c) {
-                return g_central(Dat(i, c - 2), Dat(i, c - 1), Dat(i, c + 1), Dat(i, c + 2)) * rdx;
-            };
-            auto Uy = [&](int c) {
-                return g_central(Uat(i, c - 2), Uat(i, c - 1), Uat(i, c + 1), Uat(i, c + 2)) * rdx;
-            };
-            auto Q1 = [&](int c) {
-                return g_central(Dat(i, c - 2) * Mat(i, c - 2), Dat(i, c - 1) * Mat(i, c - 1),
-                                 Dat(i, c + 1) * Mat(i, c + 1), Dat(i, c + 2) * Mat(i, c + 2)) * rdx;
-            };
-            ATy = g_central(Q1(j - 2), Q1(j - 1), Q1(j + 1), Q1(j + 2)) * rdx;
-            BTy = -g_central(Dy(j - 2) * Mat(i, j - 2), Dy(j - 1) * Mat(i, j - 1),
-                             Dy(j + 1) * Mat(i, j + 1), Dy(j + 2) * Mat(i, j + 2)) * rdx;
-            const float uy_m2 = Uy(j - 2), uy_m1 = Uy(j - 1), uy_p1 = Uy(j + 1), uy_p2 = Uy(j + 2);
-            uyy = g_central(uy_m2, uy_m1, uy_p1, uy_p2) * rdx;
-            gy = -g_central(Mat(i, j - 2) * uy_m2, Mat(i, j - 1) * uy_m1, Mat(i, j + 1) * uy_p1,
-                            Mat(i, j + 2) * uy_p2) * rdx;
+            auto Y = [&](const float *f, int d) { return f[r * AYW + c + 2 + d]; };
+            auto M = [&](int d) { return sm[(r + AHALO) * ASW + c + AHALO + d]; };
+            y.AT = g_central(Y(sqy, -2), Y(sqy, -1), Y(sqy, 1), Y(sqy, 2)) * rdx;
+            y.BT = -g_central(Y(sby, -2), Y(sby, -1), Y(sby, 1), Y(sby, 2)) * rdx;
+            y.d2 = g_central(Y(suy, -2), Y(suy, -1), Y(suy, 1), Y(suy, 2)) * rdx;
+            y.g = -g_central(M(-2) * Y(suy, -2), M(-1) * Y(suy, -1), M(1) * Y(suy, 1),
+                             M(2) * Y(suy, 2)) * rdx;
         } else {
-            auto Dy_at = [&](int c) { return fwd_d1([&](int y) { return at(D, i, y); }, c, W) * rdx; };
-            auto Uy_at = [&](int c) { return fwd_d1([&](int y) { return at(U, i, y); }, c, W) * rdx; };
-            auto Mrow = [&](int c) { return dt * __ldg(LU + (int64_t)i * pitch + c); };
-            const auto qy = make_line([&](int c) { return at(D, i, c) * Mrow(c); }, W);
-            const auto by = make_line([&](int c) { return Dy_at(c) * Mrow(c); }, W);
-            const auto gyl = make_line([&](int c) { return Mrow(c) * Uy_at(c); }, W);
-            ATy = qy.AT(j) * (rdx * rdx);
-            BTy = by.BT(j) * rdx;
-            uyy = fwd_d2([&](int c) { return at(U, i, c); }, j, W, rdx);
-            gy = gyl.BT(j) * rdx;
+            y = axis_edge<1>(a, i, j);
         }
-        const float diff_u = (ATx + ATy) + (BTx + BTy);
-        const float gD = mu * (uxx + uyy) + (gx + gy);
-        olu += diff_u;
+        const float diff_u = (x.AT + y.AT) + (x.BT + y.BT);
+        const float gD = mu * (x.d2 + y.d2) + (x.g + y.g);
         a.olv[off] = olv;
         a.olw[off] = olw;
-        a.olu[off] = olu;
+        a.olu[off] = olu + diff_u;
         if (a.gD) a.gD[off] += gD;
     }
 
     // ---- deterministic block reduction of the parameter gradients into this block's slot ----
     if (a.gtheta) {
-        __shared__ float red[kAdjParams][AB * AB / 32];
-        const int tid = threadIdx.y * AB + threadIdx.x, lane = tid & 31, warp = tid >> 5;
+        const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
         for (int k = 0; k < kAdjParams; ++k) {
             float x = gth[k];
@@ -300,7 +422,7 @@ __global__ void __launch_bounds__(AB *AB)
         __syncthreads();
         if (tid < kAdjParams) {
             double s = 0.0;
-            for (int w = 0; w < AB * AB / 32; ++w) s += (double)red[tid][w];
+            for (int w = 0; w < ANT / 32; ++w) s += (double)red[tid][w];
             a.gtheta[(int64_t)(blockIdx.y * gridDim.x + blockIdx.x) * kAdjParamStride + tid] += s;
         }
     }
@@ -308,11 +430,13 @@ __global__ void __launch_bounds__(AB *AB)
 
 }  // namespace
 
-int64_t adjoint_slots(int H, int W) { return (int64_t)((W + AB - 1) / AB) * ((H + AB - 1) / AB); }
+int64_t adjoint_slots(int H, int W) {
+    return (int64_t)((W + ATX - 1) / ATX) * ((H + ATY - 1) / ATY);
+}
 
 cudaError_t launch_adjoint(const AdjointArgs &a, cudaStream_t stream) {
-    dim3 grid((a.W + AB - 1) / AB, (a.H + AB - 1) / AB), block(AB, AB);
-    fk_adjoint_kernel<<<grid, block, 0, stream>>>(a);
+    dim3 grid((a.W + ATX - 1) / ATX, (a.H + ATY - 1) / ATY);
+    fk_adjoint_kernel<<<grid, ANT, 0, stream>>>(a);
     return cudaGetLastError();
 }
 

@@ -82,7 +82,8 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-@pytest.mark.parametrize("shape,seg", [((20, 24), None), ((48, 40), 7), ((13, 70), 30)])
+@pytest.mark.parametrize("shape,seg", [((20, 24), None), ((48, 40), 7), ((13, 70), 30),
+                                       ((64, 72), 16)])
 def test_adjoint_matches_fp64_autodiff(shape, seg):
     _gpu()
     case = _case(shape, sum(shape))
