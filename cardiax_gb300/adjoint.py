@@ -14,6 +14,8 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
+from concurrent.futures import ThreadPoolExecutor
 from typing import Sequence
 
 import torch
@@ -204,9 +206,21 @@ def rollout(v0, w0, u0, D, theta, stimuli, t0: int, t1: int, obs_times: Sequence
                           int(t1), list(obs_times), float(dt), float(dx), seg)
 
 
+def _per_experiment(fn, n: int):
+    """Runs fn(b) for b in 0..n-1 from a pool of host threads.  Each experiment's steps are
+    C loops that release the GIL, so the experiments' launches are issued in parallel (one
+    thread issuing thousands of small launches is what bounds a batch of small tissues)."""
+    workers = max(1, min(n, os.cpu_count() or 1))
+    if workers == 1:
+        return [fn(b) for b in range(n)]
+    with ThreadPoolExecutor(workers) as ex:
+        return list(ex.map(fn, range(n)))
+
+
 class _RolloutBatch(torch.autograd.Function):
     """States at ``obs_times`` of B tissues sharing D and theta (one stimulus list per tissue);
-    each tissue's forward and backward run on its own CUDA stream so the GPU overlaps them."""
+    each tissue's forward and backward run on its own CUDA stream, issued from its own host
+    thread, so the GPU overlaps them."""
 
     @staticmethod
     def forward(ctx, states0, D, theta, Cm, stimuli, t0, t1, obs_times, dt, dx, seg):
@@ -218,22 +232,26 @@ class _RolloutBatch(torch.autograd.Function):
         out = torch.empty((B, len(obs_times), 3, H, W), dtype=torch.float32, device=dev)
         main = torch.cuda.current_stream(dev)
         streams = [torch.cuda.Stream(dev) for _ in range(B)]
-        tissues, ckpts, state0s = [], [], []
-        for b in range(B):
+        Dd = D.detach()
+
+        def one(b):
             streams[b].wait_stream(main)
-            with torch.cuda.stream(streams[b]):
-                tis = Tissue((H, W), params, D.detach(), stimuli[b], dt=dt, dx=dx, device=dev)
+            with torch.cuda.device(dev), torch.cuda.stream(streams[b]):
+                tis = Tissue((H, W), params, Dd, stimuli[b], dt=dt, dx=dx, device=dev)
                 tis.set_state(states0[b].detach())
                 s0 = tis.state.clone()
                 ck, snaps = forward_checkpoints(tis, s0, t0, t_end, seg, stops=list(obs_times))
                 for k, t in enumerate(obs_times):
                     out[b, k] = snaps[int(t)]
-            tissues.append(tis)
-            ckpts.append(ck)
-            state0s.append(s0)
+            return tis, ck, s0
+
+        res = _per_experiment(one, B)
         for s in streams:
             main.wait_stream(s)
-        ctx.tissues, ctx.ckpts, ctx.state0s, ctx.streams = tissues, ckpts, state0s, streams
+        ctx.tissues = [r[0] for r in res]
+        ctx.ckpts = [r[1] for r in res]
+        ctx.state0s = [r[2] for r in res]
+        ctx.streams = streams
         ctx.t0, ctx.t1, ctx.obs_times, ctx.seg, ctx.W = t0, t_end, list(obs_times), seg, W
         return out
 
@@ -242,24 +260,27 @@ class _RolloutBatch(torch.autograd.Function):
         W = ctx.W
         main = torch.cuda.current_stream()
         B = len(ctx.tissues)
-        g0 = []
-        adjs = []
-        for b in range(B):
+        grad_out = grad_out.contiguous()
+
+        def one(b):
             s = ctx.streams[b]
             s.wait_stream(main)
-            with torch.cuda.stream(s):
-                tis = ctx.tissues[b]
+            tis = ctx.tissues[b]
+            with torch.cuda.device(tis.device), torch.cuda.stream(s):
                 adj = Adjoint(tis)
                 g = torch.zeros((len(ctx.obs_times),) + tuple(ctx.state0s[b].shape),
                                 dtype=torch.float32, device=tis.device)
                 g[..., :W] = grad_out[b].to(torch.float32)
                 lam0 = adj.rollout_gradient(ctx.state0s[b], ctx.t0, ctx.t1, ctx.obs_times, g,
                                             seg=ctx.seg, ckpts=ctx.ckpts[b])
-                g0.append(lam0[:, :, :W])
-                adjs.append(adj)
+            return lam0[:, :, :W], adj
+
+        res = _per_experiment(one, B)
         for s in ctx.streams:
             main.wait_stream(s)
         ctx.ckpts = None
+        g0 = [r[0] for r in res]
+        adjs = [r[1] for r in res]
         gD = adjs[0].grad_D().clone()
         gth = adjs[0].grad_theta()
         for a in adjs[1:]:  # fixed order: deterministic sums
