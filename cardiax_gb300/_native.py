@@ -85,6 +85,8 @@ _SIGNATURES = {
                      _D, _D, _P, _P, _P],
     "fk_forward_heun": [Grid, _P, _P, _P, ctypes.POINTER(Params), ctypes.POINTER(Stimulus), _INT,
                         _I64, _I64, _D, _D, _P],
+    "fk_resize_bilinear": [_P, _I64, _I64, _I64, _I64, _P, _I64, _I64, _I64, _INT, _P],
+    "fk_rotate_field": [_P, _I64, _I64, _I64, _P, _I64, _D, _P],
     "fk_batch_create": [ctypes.POINTER(TissueDesc), _INT, _P, ctypes.c_size_t, _P,
                         ctypes.POINTER(_P)],
     "fk_batch_forward_euler": [_P, _I64, _I64, _INT, _P],

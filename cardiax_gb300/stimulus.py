@@ -74,12 +74,19 @@ def linear(shape: Shape, direction: Direction, coverage: float, modulus: float,
 
 def triangular(shape: Shape, direction: Direction, angle: float, coverage: float,
                modulus: float, protocol: Protocol, device=None) -> Stimulus:
-    """``linear`` rotated by ``angle`` degrees with nearest-edge filling and no prefilter
-    (cardiax/stimulus.py:109-140).  Host-side set-up through SciPy."""
-    from scipy.ndimage import rotate
+    """``linear`` rotated by ``angle`` degrees about the centre (cardiax/stimulus.py:109-140):
+    the reference's scipy.ndimage.rotate(mode="nearest", prefilter=False, reshape=False), as a
+    CUDA kernel (``fk_rotate_field``)."""
+    from . import _native as N
+    from .tissue import stream_handle
 
-    stim = linear(shape, direction, coverage, modulus, protocol, device="cpu")
-    field = rotate(stim.field.numpy(), angle=angle, mode="nearest", prefilter=False,
-                   reshape=False)
-    return Stimulus(protocol, torch.as_tensor(np.ascontiguousarray(field, dtype=np.float32),
-                                              device=_device(device)))
+    dev = _device(device)
+    if dev.type != "cuda":
+        raise RuntimeError("triangular fields are built on a CUDA device (there is no CPU path)")
+    stim = linear(shape, direction, coverage, modulus, protocol, device=dev)
+    src = stim.field.to(device=dev, dtype=torch.float32).contiguous()
+    H, W = int(src.shape[0]), int(src.shape[1])
+    out = torch.empty_like(src)
+    N.call("fk_rotate_field", src.data_ptr(), H, W, W, out.data_ptr(), W, float(angle),
+           stream_handle())
+    return Stimulus(protocol, out)

@@ -172,6 +172,22 @@ int fk_forward_flow(fk_grid g, const float *state0, float *scratch, const float 
                     const int64_t *checkpoints, int n_checkpoints, double dt, double dx,
                     float *out, int32_t *flags, int64_t n_flags, void *stream);
 
+/* ---- checkpoint emission ----------------------------------------------------------------------
+ * io.imresize (cardiax/io.py:118-124), which the data-generation caller applies to every
+ * checkpoint (deepx/generate.py:187-199): `planes` float32 planes of H x W (row pitch in_pitch,
+ * planes H * in_pitch apart) resized to OH x OW (out_pitch, planes OH * out_pitch apart) with
+ * the bilinear (triangle-kernel, half-pixel-centre) resampling of jax.image.resize, widened when
+ * downsampling if `antialias` (jax.image.resize's default). */
+int fk_resize_bilinear(const float *in, int64_t planes, int64_t H, int64_t W, int64_t in_pitch,
+                       float *out, int64_t OH, int64_t OW, int64_t out_pitch, int antialias,
+                       void *stream);
+
+/* stimulus.triangular (cardiax/stimulus.py:109-140): the H x W plane `in` rotated by `angle_deg`
+ * degrees about its centre into `out` (a separate plane) as scipy.ndimage.rotate(mode="nearest",
+ * prefilter=False, reshape=False) does: order-3 B-spline of the samples, edge-replicated. */
+int fk_rotate_field(const float *in, int64_t H, int64_t W, int64_t pitch, float *out,
+                    int64_t out_pitch, double angle_deg, void *stream);
+
 /* ---- many tissues in one launch --------------------------------------------------------------
  * No reference counterpart: the reference steps one tissue per call (its data generation loops
  * over tissues in Python, deepx/generate.py:135-210).  Here every tissue of a batch advances in

@@ -17,6 +17,14 @@ round the same way):
 * ``cardiax/solve.py:257-271`` ``stimulate``  -> :func:`stimulate`
 * ``cardiax/stimulus.py:63-106,31-60`` ``linear``/``rectangular`` -> :func:`linear_field`,
   :func:`rectangular_field`
+* ``cardiax/stimulus.py:109-140`` ``triangular`` -> :func:`rotate_field` (the reference's
+  ``scipy.ndimage.rotate(mode="nearest", prefilter=False, reshape=False)`` restated; pinned to
+  SciPy itself in ``tests/test_oracle.py``)
+* ``cardiax/io.py:118-124`` ``imresize`` -> :func:`imresize_bilinear` (the reference calls
+  ``jax.image.resize(a, shape, "bilinear")``; JAX, pinned through jaxlib 0.1.64 in
+  ``install_jax.sh``, is not vendored and cannot be installed here, so this is a restatement of
+  its published resampling algorithm -- parity unpinned, checked on known answers of the
+  triangle kernel in ``tests/test_oracle.py``)
 
 Pinning: the float32 path is checked bit for bit against golden vectors produced by running
 the reference's own ``solve.py`` (under a NumPy stand-in for JAX, see
@@ -213,3 +221,63 @@ def rectangular_field(shape, centre, size, modulus: float, dtype=np.float32):
     y1, y2 = int(centre[1] - size[1] / 2), int(centre[1] + size[1] / 2)
     a[x1:x2, y1:y2] = modulus
     return a
+
+
+# --- bilinear resize (cardiax/io.py:118-124 -> jax.image.resize "bilinear") -------------------
+def resize_weights(n_in: int, n_out: int, antialias: bool = True) -> np.ndarray:
+    """(n_in, n_out) float32 weights of one resized axis: the triangle kernel max(0, 1 - |x|)
+    at half-pixel centres, output p sampling s = (p + 0.5) / scale - 0.5 (scale = n_out /
+    n_in), widened by 1 / scale when downsampling with ``antialias``, normalised per output."""
+    f = np.float32
+    inv = f(1.0 / (n_out / n_in))
+    ks = max(inv, f(1)) if antialias else f(1)
+    s = (np.arange(n_out, dtype=f) + f(0.5)) * inv - f(0.5)
+    x = np.abs(s[None, :] - np.arange(n_in, dtype=f)[:, None]) / ks
+    w = np.maximum(f(0), f(1) - x)
+    tot = w.sum(0, keepdims=True, dtype=f)
+    w = np.where(np.abs(tot) > f(1000) * np.finfo(f).eps, w / np.where(tot != 0, tot, f(1)), f(0))
+    valid = (s >= f(-0.5)) & (s <= f(n_in) - f(0.5))
+    return np.where(valid[None, :], w, f(0)).astype(f)
+
+
+def imresize_bilinear(a: np.ndarray, size, antialias: bool = True) -> np.ndarray:
+    """The last two axes of ``a`` resized to ``size``; an axis whose size does not change is
+    left as it is."""
+    out = np.asarray(a, dtype=np.float32)
+    H, W = out.shape[-2:]
+    if int(size[0]) != H:
+        out = np.einsum("...hw,ho->...ow", out, resize_weights(H, int(size[0]), antialias))
+    if int(size[1]) != W:
+        out = np.einsum("...hw,wo->...ho", out, resize_weights(W, int(size[1]), antialias))
+    return out.astype(np.float32)
+
+
+# --- rotated fields (cardiax/stimulus.py:109-140 -> scipy.ndimage.rotate) ----------------------
+def _bspline3(t):
+    t = np.abs(t)
+    return np.where(t < 1, 2.0 / 3.0 - t * t + 0.5 * t ** 3, np.where(t < 2, (2 - t) ** 3 / 6, 0.0))
+
+
+def rotate_field(a: np.ndarray, angle: float) -> np.ndarray:
+    """``a`` rotated by ``angle`` degrees about its centre: output (i, j) samples (x, y) =
+    R (i, j) + o, R = [[c, s], [-s, c]], o = (n-1)/2 - R (n-1)/2, with the order-3 B-spline
+    of the samples (no prefilter) and edge-replicated indices; float64 inside, float32 out."""
+    a = np.asarray(a, dtype=np.float32)
+    H, W = a.shape
+    r = float(angle) % 360.0
+    exact = {0.0: (1.0, 0.0), 90.0: (0.0, 1.0), 180.0: (-1.0, 0.0), 270.0: (0.0, -1.0)}
+    c, s = exact.get(r, (np.cos(np.deg2rad(angle)), np.sin(np.deg2rad(angle))))
+    ch, cw = (H - 1) / 2.0, (W - 1) / 2.0
+    o0, o1 = ch - (c * ch + s * cw), cw - (-s * ch + c * cw)
+    i, j = np.meshgrid(np.arange(H, dtype=np.float64), np.arange(W, dtype=np.float64),
+                       indexing="ij")
+    x, y = c * i + s * j + o0, -s * i + c * j + o1
+    i0, j0 = np.floor(x).astype(np.int64) - 1, np.floor(y).astype(np.int64) - 1
+    acc = np.zeros((H, W))
+    for p in range(4):
+        wx = _bspline3(x - (i0 + p))
+        ii = np.clip(i0 + p, 0, H - 1)
+        for q in range(4):
+            jj = np.clip(j0 + q, 0, W - 1)
+            acc += wx * _bspline3(y - (j0 + q)) * a[ii, jj]
+    return acc.astype(np.float32)

@@ -110,3 +110,48 @@ def test_heun_golden(golden, tag, dtype):
                          0.01, 0.01)
     for name, arr in zip("vwu", res):
         np.testing.assert_array_equal(arr, h[f"{name}_{tag}"])
+
+
+# --- bilinear resize (restatement of jax.image.resize "bilinear"; known answers) --------------
+def test_resize_identity_and_constant():
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((3, 17, 23)).astype(np.float32)
+    assert np.array_equal(O.imresize_bilinear(a, (17, 23)), a)
+    c = np.full((2, 40, 30), 0.7, np.float32)
+    for size in ((20, 15), (13, 7), (80, 61), (40, 11)):
+        np.testing.assert_allclose(O.imresize_bilinear(c, size), 0.7, rtol=1e-6)
+
+
+def test_resize_triangle_kernel_known_weights():
+    # 2x downsampling with antialiasing: the kernel widens to radius 2, interior weights
+    # (1, 3, 3, 1) / 8 on inputs 2p-1 .. 2p+2; the first output renormalises (3, 3, 1) / 7
+    w = O.resize_weights(16, 8, antialias=True)
+    np.testing.assert_allclose(w[3:7, 2], np.array([1, 3, 3, 1]) / 8, rtol=1e-6)
+    np.testing.assert_allclose(w[0:3, 0], np.array([3, 3, 1]) / 7, rtol=1e-6)
+    # without antialiasing 2x downsampling averages the two nearest inputs
+    w = O.resize_weights(16, 8, antialias=False)
+    np.testing.assert_allclose(w[4:6, 2], [0.5, 0.5], rtol=1e-6)
+    # 2x upsampling: output p samples p/2 - 1/4 -> (3/4, 1/4) blends, first output = input 0
+    w = O.resize_weights(8, 16)
+    np.testing.assert_allclose(w[0:2, 1], [0.75, 0.25], rtol=1e-6)
+    np.testing.assert_allclose(w[:, 0], np.eye(8)[0], rtol=1e-6)
+
+
+def test_resize_linear_ramp_upsampling_is_exact_inside():
+    a = np.tile(np.arange(10, dtype=np.float32), (4, 1))
+    b = O.imresize_bilinear(a, (4, 20))
+    p = np.arange(1, 19)
+    np.testing.assert_allclose(b[0, p], p / 2 - 0.25, atol=1e-6)
+
+
+@pytest.mark.parametrize("shape,angle", [((20, 24), 30.0), ((17, 13), 47.5), ((16, 16), 90.0),
+                                         ((21, 30), -12.3), ((40, 40), 180.0), ((33, 64), 721.0)])
+def test_rotate_field_matches_scipy(shape, angle):
+    """The restatement of stimulus.triangular's rotation against SciPy itself."""
+    from scipy.ndimage import rotate
+    rng = np.random.default_rng(sum(shape) + abs(int(angle)))
+    stripe = np.zeros(shape, np.float32)
+    stripe[:, : max(1, shape[1] // 5)] = 20.0
+    for a in (stripe, rng.uniform(0, 1, shape).astype(np.float32)):
+        ref = rotate(a, angle=angle, mode="nearest", prefilter=False, reshape=False)
+        np.testing.assert_allclose(O.rotate_field(a, angle), ref, rtol=1e-6, atol=1e-6)
