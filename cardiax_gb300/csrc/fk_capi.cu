@@ -25,6 +25,7 @@
 #include "fk_capi_internal.h"
 #include "fk_adjoint.cuh"
 #include "fk_step.cuh"
+#include "fk_strip.cuh"
 #include "fk_tb.cuh"
 
 namespace fk {
@@ -140,8 +141,10 @@ int make_stims(const fk_stimulus *s, int n, const fk_grid &g, Stim *out) {
 struct MapCache {
     static constexpr int kSlots = 4;
     const float *ptr[kSlots] = {nullptr, nullptr, nullptr, nullptr};
-    CUtensorMap u[kSlots], v[kSlots], w[kSlots], ut[kSlots];
+    CUtensorMap u[kSlots], v[kSlots], w[kSlots], ut[kSlots], us[kSlots];
     int next = 0;
+    const float *dptr = nullptr;  // D plane of `ds`
+    CUtensorMap ds;               // D with the strip kernel's box
     // slot of `state`, building its maps if needed without evicting slot `keep`
     int lookup(const fk_grid &g, const float *state, int keep, int *slot) {
         for (int i = 0; i < kSlots; ++i)
@@ -158,7 +161,8 @@ struct MapCache {
         if ((rc = make_plane_map(&u[k], state + 2 * plane, g.H, g.W, g.pitch, SW, SU_H)) ||
             (rc = make_plane_map(&v[k], state, g.H, g.W, g.pitch, TX, TY)) ||
             (rc = make_plane_map(&w[k], state + plane, g.H, g.W, g.pitch, TX, TY)) ||
-            (rc = make_plane_map(&ut[k], state + 2 * plane, g.H, g.W, g.pitch, TX, TY)))
+            (rc = make_plane_map(&ut[k], state + 2 * plane, g.H, g.W, g.pitch, TX, TY)) ||
+            (rc = make_plane_map(&us[k], state + 2 * plane, g.H, g.W, g.pitch, S_SW, S_UH)))
             return rc;
         ptr[k] = state;
         *slot = k;
@@ -174,7 +178,24 @@ struct MapCache {
         sm.ou = ut[ko];
         return FK_OK;
     }
+    // maps of a strip-kernel step reading `in` with diffusivity `D`
+    int get_strip(const fk_grid &g, const float *in, const float *D, StripMaps &sm) {
+        int ki, rc;
+        if ((rc = lookup(g, in, -1, &ki))) return rc;
+        if (dptr != D) {
+            dptr = nullptr;
+            if ((rc = make_plane_map(&ds, D, g.H, g.W, g.pitch, S_SW, S_DH))) return rc;
+            dptr = D;
+        }
+        sm.u = us[ki];
+        sm.d = ds;
+        return FK_OK;
+    }
 };
+
+// Which kernel takes an Euler step: 0 = the tiled kernel (fk_step_kernel, default), 1 = the
+// strip kernel wherever it applies.  Set through fk_select_step_kernel.
+static int g_step_kernel = 0;
 
 // One step from `in` to `out` (Euler, or the derivative with `deriv`).
 int step_once(const fk_grid &g, const float *in, float *out, const float *D, const Model &m,
@@ -210,7 +231,14 @@ int step_once(const fk_grid &g, const float *in, float *out, const float *D, con
         a.act_count = act->count;
         a.act_threshold = act->threshold;
     }
-    cudaError_t e = launch_step(sm, a, deriv, stream);
+    cudaError_t e;
+    if (!deriv && g_step_kernel == 1 && strip_eligible(g.H, g.W)) {
+        StripMaps xm;
+        if ((rc = maps.get_strip(g, in, D, xm))) return rc;
+        e = launch_strip(xm, a, stream);
+    } else {
+        e = launch_step(sm, a, deriv, stream);
+    }
     return e == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
 
@@ -353,6 +381,12 @@ const char *fk_status_string(int s) {
                    "(H * pitch must be <= FK_NOALLOC_MAX_CELLS = 512 * 512)";
         default: return "unknown status";
     }
+}
+
+int fk_select_step_kernel(int which) {
+    if (which != 0 && which != 1) return FK_ERR_ARGUMENT;
+    g_step_kernel = which;
+    return FK_OK;
 }
 
 int fk_device_status(int reset, int *value) {

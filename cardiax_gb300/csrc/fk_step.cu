@@ -8,10 +8,60 @@
 
 namespace fk {
 
+// ---- tile order ------------------------------------------------------------------------------
+// Edge tiles (those that take the clamped-halo path) cost more than interior tiles.  Handing
+// them out first, one per CTA, keeps the persistent CTAs balanced; a plain row-major
+// round-robin gives every 16th CTA an edge tile on every other turn.
+struct TileOrder {
+    int nc, r_lo, r_hi, c_lo, c_hi;  // interior tile rows [r_lo, r_hi], columns [c_lo, c_hi]
+    int n_top, n_mid_row, n_mid, n_edge;
+    __device__ TileOrder(int H, int W) {
+        const int nr = (H + TY - 1) / TY;
+        nc = (W + TX - 1) / TX;
+        r_lo = (BAND + TY - 1) / TY;
+        r_hi = (H - BAND) / TY - 1;
+        c_lo = (BAND + TX - 1) / TX;
+        c_hi = (W - BAND) / TX - 1;
+        if (r_hi < r_lo || c_hi < c_lo) {  // no interior tile: plain row-major order
+            r_lo = nr;
+            r_hi = nr - 1;
+            c_lo = 0;
+            c_hi = nc - 1;
+        }
+        n_top = r_lo * nc;
+        n_mid_row = c_lo + (nc - 1 - c_hi);
+        n_mid = (r_hi - r_lo + 1) * n_mid_row;
+        n_edge = nr * nc - (r_hi - r_lo + 1) * (c_hi - c_lo + 1);
+    }
+    // tile row and column of the k-th tile handed out
+    __device__ void at(int k, int &tr, int &tc) const {
+        if (k < n_edge) {
+            if (k < n_top) {
+                tr = k / nc;
+                tc = k % nc;
+            } else if (k < n_top + n_mid) {
+                const int m = k - n_top;
+                tr = r_lo + m / n_mid_row;
+                const int q = m % n_mid_row;
+                tc = q < c_lo ? q : c_hi + 1 + (q - c_lo);
+            } else {
+                const int m = k - n_top - n_mid;
+                tr = r_hi + 1 + m / nc;
+                tc = m % nc;
+            }
+        } else {
+            const int m = k - n_edge, w = c_hi - c_lo + 1;
+            tr = r_lo + m / w;
+            tc = c_lo + m % w;
+        }
+    }
+};
+
 // ---- the step kernel: persistent CTAs over the tiles of one tissue ------------------------
 template <bool DERIV, bool ACT>
 __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_constant__ StepMaps tm,
-                                                        const __grid_constant__ StepArgs a) {
+                                                        const __grid_constant__ StepArgs a,
+                                                        const __grid_constant__ PackConsts k) {
     extern __shared__ unsigned char smem_raw[];
     // 128-byte aligned base, offset as a pointer so that the compiler keeps the shared-memory
     // state space (integer address arithmetic would turn every access into a generic one)
@@ -38,8 +88,17 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
     // the previous step's grid (same stream) must have finished writing our input state
     grid_dependency_wait();
     grid_launch_dependents();
-    auto tile_i0 = [&](int tl) { return (tl / ntx) * TY; };
-    auto tile_j0 = [&](int tl) { return (tl % ntx) * TX; };
+    const TileOrder order(a.H, a.W);
+    auto tile_i0 = [&](int tl) {
+        int tr, tc;
+        order.at(tl, tr, tc);
+        return tr * TY;
+    };
+    auto tile_j0 = [&](int tl) {
+        int tr, tc;
+        order.at(tl, tr, tc);
+        return tc * TX;
+    };
     int tile = blockIdx.x;
     if (tid == 0)  // prologue: the first two tiles of this CTA
         for (int k = 0; k < NSTAGE - 1; ++k) {
@@ -70,8 +129,8 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
         auto outputs_free = [&] {
             if (threadIdx.x == 0) bulk_wait_read();
         };
-        process_tile<DERIV, ACT>(*sa, a.t, stage_at(smem, s), sux, suy, io, active, i0, j0,
-                                 outputs_free);
+        process_tile<DERIV, ACT, true>(*sa, a.t, stage_at(smem, s), sux, suy, io, active, i0, j0,
+                                       outputs_free, &k);
         store_tile(tm, io, i0, j0);  // its barrier also frees sux, suy and stage s
     }
     if (tid == 0) bulk_wait_all();
@@ -239,9 +298,10 @@ cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cud
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (deriv) return cudaLaunchKernelEx(&cfg, fk_step_kernel<true, false>, maps, a);
-    if (a.act_last) return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, true>, maps, a);
-    return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, false>, maps, a);
+    const PackConsts k = make_pack_consts(a.m, a.rdx, a.dt);
+    if (deriv) return cudaLaunchKernelEx(&cfg, fk_step_kernel<true, false>, maps, a, k);
+    if (a.act_last) return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, true>, maps, a, k);
+    return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, false>, maps, a, k);
 }
 
 }  // namespace fk

@@ -16,7 +16,12 @@
 //
 // State planes are read with L2-coherent loads (ld.global.cg), never through the read-only
 // path: in the dataflow kernel they are rewritten by other CTAs while the kernel runs.
+//
+// PK selects packed arithmetic (two cells per FP32 instruction, fk_pack.cuh) for every stencil
+// whose formula is uniform across a thread's 4 columns, the reaction, the diffusion sum and the
+// Euler update; it needs the launch's PackConsts.  Both modes produce the same bits.
 #pragma once
+#include "fk_pack.cuh"
 #include "fk_ptx.cuh"
 #include "fk_step.cuh"
 
@@ -261,10 +266,11 @@ static __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_ro
 // EDGE: the tile touches the grid edge (and is not a one-row or one-column sliver): the halo
 // is clamped and every derivative picks the reference's row type, exactly as the padded
 // arrays of cardiax/solve.py:29-32,49-54 do.
-template <bool DERIV, bool ACT, bool EDGE, class P1>
-__device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const Stage &st,
-                                             float *sux, float *suy, const TileIO &io,
-                                             unsigned active, int i0, int j0, P1 &&after_pass1) {
+template <bool DERIV, bool ACT, bool EDGE, bool PK, class P1>
+__device__ __forceinline__ void compute_tile(const StepArgs &a, const PackConsts *pk, float t,
+                                             const Stage &st, float *sux, float *suy,
+                                             const TileIO &io, unsigned active, int i0, int j0,
+                                             P1 &&after_pass1) {
     const int tid = threadIdx.x;
     const int H = a.H, W = a.W, pitch = a.pitch;
     const float rdx = a.rdx;
@@ -281,6 +287,21 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
     for (int it = tid; it < SUX_H * NTX; it += NT) {
         const int r = it / NTX, q = it % NTX;
         const float *b = su + (r + 2) * SW + HALO_U + 4 * q;  // u row of ux row r
+        if constexpr (PK) {
+            const PackConsts &kc = *pk;
+            Quad o;
+            const int x = i0 - 2 + r;  // global row of this u_x row
+            if (!EDGE || (x > 0 && x < H - 1))
+                o = q_central(kc, ld_quad(b - 2 * SW), ld_quad(b - SW), ld_quad(b + SW),
+                              ld_quad(b + 2 * SW));
+            else if (x <= 0)
+                o = q_head(kc, ld_quad(b), ld_quad(b + SW), ld_quad(b + 2 * SW), ld_quad(b + 3 * SW));
+            else
+                o = q_tail(kc, ld_quad(b - 3 * SW), ld_quad(b - 2 * SW), ld_quad(b - SW), ld_quad(b));
+            o = q_scale(o, kc.rdx);
+            st4(sux + r * TX + 4 * q, make_float4(o.lo.x, o.lo.y, o.hi.x, o.hi.y));
+            continue;
+        }
         float4 o;
         if (!EDGE) {
             o = g_central4(ld4(b - 2 * SW), ld4(b - SW), ld4(b + SW), ld4(b + 2 * SW));
@@ -310,20 +331,29 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
         const float4 x0 = ld4(b), x1 = ld4(b + 4), x2 = ld4(b + 8);
         const float e[12] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
                              x2.x, x2.y, x2.z, x2.w};
-        float o[4];
+        if constexpr (PK && !EDGE) {
+            const PackConsts &kc = *pk;  // u_y at columns c .. c+3 as the pairs (c, c+1), (c+2, c+3)
+            const float2 lo = p_mul(pg_central(kc, mk2(e[2], e[3]), mk2(e[3], e[4]),
+                                               mk2(e[5], e[6]), mk2(e[6], e[7])), kc.rdx);
+            const float2 hi = p_mul(pg_central(kc, mk2(e[4], e[5]), mk2(e[5], e[6]),
+                                               mk2(e[7], e[8]), mk2(e[8], e[9])), kc.rdx);
+            st4(suy + r * SW + HALO_U + 4 * q, make_float4(lo.x, lo.y, hi.x, hi.y));
+        } else {
+            float o[4];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            if (!EDGE) {
-                o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
-            } else {  // u_y at padded position y: head / tail / central row of the padded line
-                const int y = j0 + 4 * q + m;
-                if (y <= 0) o[m] = g_head(e[m + 4], e[m + 5], e[m + 6], e[m + 7]);
-                else if (y >= W - 1) o[m] = g_tail(e[m + 1], e[m + 2], e[m + 3], e[m + 4]);
-                else o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
+            for (int m = 0; m < 4; ++m) {
+                if (!EDGE) {
+                    o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
+                } else {  // u_y at padded position y: head / tail / central row of the padded line
+                    const int y = j0 + 4 * q + m;
+                    if (y <= 0) o[m] = g_head(e[m + 4], e[m + 5], e[m + 6], e[m + 7]);
+                    else if (y >= W - 1) o[m] = g_tail(e[m + 1], e[m + 2], e[m + 3], e[m + 4]);
+                    else o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
+                }
             }
+            st4(suy + r * SW + HALO_U + 4 * q,
+                make_float4(o[0] * rdx, o[1] * rdx, o[2] * rdx, o[3] * rdx));
         }
-        st4(suy + r * SW + HALO_U + 4 * q,
-            make_float4(o[0] * rdx, o[1] * rdx, o[2] * rdx, o[3] * rdx));
     }
     if (tid >= NT - TY * 4) {  // the 2 + 2 halo columns of u_y (threads with one ux item less)
         const int h = tid - (NT - TY * 4);
@@ -352,6 +382,119 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, float t, const S
         const int r = RPT * ty + k;
         const int i = i0 + r;
         const int64_t goff = (int64_t)i * pitch + j;
+        if constexpr (PK) {
+            const PackConsts &kc = *pk;
+            const float *xb = sux + (r + 2) * TX + 4 * tx;
+            const float *db = sd + (r + HALO_D) * SW + HALO_U + 4 * tx;
+            const Quad uxc = ld_quad(xb), dcq = ld_quad(db);
+            Quad uxx, dxD;
+            if (!EDGE || (i != 0 && i != H - 1)) {
+                uxx = q_central(kc, ld_quad(xb - 2 * TX), ld_quad(xb - TX), ld_quad(xb + TX),
+                                ld_quad(xb + 2 * TX));
+                dxD = q_central(kc, ld_quad(db - 2 * SW), ld_quad(db - SW), ld_quad(db + SW),
+                                ld_quad(db + 2 * SW));
+            } else if (i == 0) {  // head rows on u_x rows 0..3 and D rows 0..3
+                uxx = q_head(kc, uxc, ld_quad(xb + TX), ld_quad(xb + 2 * TX), ld_quad(xb + 3 * TX));
+                dxD = q_head(kc, dcq, ld_quad(db + SW), ld_quad(db + 2 * SW), ld_quad(db + 3 * SW));
+            } else {  // i == H-1: tail rows on rows H-4 .. H-1
+                uxx = q_tail(kc, ld_quad(xb - 3 * TX), ld_quad(xb - 2 * TX), ld_quad(xb - TX), uxc);
+                dxD = q_tail(kc, ld_quad(db - 3 * SW), ld_quad(db - 2 * SW), ld_quad(db - SW), dcq);
+            }
+            uxx = q_scale(uxx, kc.rdx);
+            dxD = q_scale(dxD, kc.rdx);
+            const float *yb = suy + r * SW + 4 * tx;
+            const float4 y0 = ld4(yb), y1 = ld4(yb + 4), y2 = ld4(yb + 8);
+            const float4 dl = ld4(db - 4), dr = ld4(db + 4);
+            const float4 uc = ld4(su + (r + HALO_U) * SW + HALO_U + 4 * tx);
+            const float4 vc = io.v[k], wc = io.w[k];
+            const float f[12] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w,
+                                 y2.x, y2.y, y2.z, y2.w};  // u_y at columns j-4 .. j+7
+            const float g[12] = {dl.x, dl.y, dl.z, dl.w, dcq.lo.x, dcq.lo.y, dcq.hi.x, dcq.hi.y,
+                                 dr.x, dr.y, dr.z, dr.w};  // D at columns j-4 .. j+7
+            float2 uyy_lo, uyy_hi, dyD_lo, dyD_hi;
+            if (!EDGE) {
+                uyy_lo = p_mul(pg_central(kc, mk2(f[2], f[3]), mk2(f[3], f[4]), mk2(f[5], f[6]),
+                                          mk2(f[6], f[7])), kc.rdx);
+                uyy_hi = p_mul(pg_central(kc, mk2(f[4], f[5]), mk2(f[5], f[6]), mk2(f[7], f[8]),
+                                          mk2(f[8], f[9])), kc.rdx);
+                dyD_lo = p_mul(pg_central(kc, mk2(g[2], g[3]), mk2(g[3], g[4]), mk2(g[5], g[6]),
+                                          mk2(g[6], g[7])), kc.rdx);
+                dyD_hi = p_mul(pg_central(kc, mk2(g[4], g[5]), mk2(g[5], g[6]), mk2(g[7], g[8]),
+                                          mk2(g[8], g[9])), kc.rdx);
+            } else {  // second derivative / D_y at column y: head at 0, tail at W-1
+                float uy4[4], dy4[4];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    const int y = j + m;
+                    float uyy, dyD;
+                    if (y == 0) {
+                        uyy = g_head(f[m + 4], f[m + 5], f[m + 6], f[m + 7]);
+                        dyD = g_head(g[m + 4], g[m + 5], g[m + 6], g[m + 7]);
+                    } else if (y == W - 1) {
+                        uyy = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]);
+                        dyD = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]);
+                    } else {
+                        uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
+                        dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
+                    }
+                    uy4[m] = uyy * rdx;
+                    dy4[m] = dyD * rdx;
+                }
+                uyy_lo = mk2(uy4[0], uy4[1]);
+                uyy_hi = mk2(uy4[2], uy4[3]);
+                dyD_lo = mk2(dy4[0], dy4[1]);
+                dyD_hi = mk2(dy4[2], dy4[3]);
+            }
+            const float2 u_lo = mk2(uc.x, uc.y), u_hi = mk2(uc.z, uc.w);
+            const float2 v_lo = mk2(vc.x, vc.y), v_hi = mk2(vc.z, vc.w);
+            const float2 w_lo = mk2(wc.x, wc.y), w_hi = mk2(wc.z, wc.w);
+            const PairReaction rl = p_reaction(kc, a.m, u_lo, v_lo, w_lo);
+            const PairReaction rh = p_reaction(kc, a.m, u_hi, v_hi, w_hi);
+            float2 j_lo = rl.j_ion, j_hi = rh.j_ion;
+            if (active) {
+                const float4 js = apply_stimuli(a, active, i, j, goff,
+                                                make_float4(j_lo.x, j_lo.y, j_hi.x, j_hi.y));
+                j_lo = mk2(js.x, js.y);
+                j_hi = mk2(js.z, js.w);
+            }
+            // del u = D (u_xx + u_yy) + D_x u_x + D_y u_y, du = del u + J, with no packed
+            // multiply feeding a packed add (fk_pack.cuh: contraction hazard)
+            float2 du_lo = p_mul(dcq.lo, add_products(uxx.lo, uyy_lo));
+            du_lo = p_fma(dxD.lo, uxc.lo, du_lo);
+            du_lo = p_fma(dyD_lo, mk2(f[4], f[5]), du_lo);
+            du_lo = p_add_product(kc, du_lo, j_lo);
+            float2 du_hi = p_mul(dcq.hi, add_products(uxx.hi, uyy_hi));
+            du_hi = p_fma(dxD.hi, uxc.hi, du_hi);
+            du_hi = p_fma(dyD_hi, mk2(f[6], f[7]), du_hi);
+            du_hi = p_add_product(kc, du_hi, j_hi);
+            float2 nv_lo, nv_hi, nw_lo, nw_hi, nu_lo, nu_hi;
+            if (DERIV) {
+                nv_lo = rl.dv;
+                nv_hi = rh.dv;
+                nw_lo = rl.dw;
+                nw_hi = rh.dw;
+                nu_lo = du_lo;
+                nu_hi = du_hi;
+            } else {
+                nv_lo = p_fma(rl.dv, kc.dt, v_lo);
+                nv_hi = p_fma(rh.dv, kc.dt, v_hi);
+                nw_lo = p_fma(rl.dw, kc.dt, w_lo);
+                nw_hi = p_fma(rh.dw, kc.dt, w_hi);
+                nu_lo = p_fma(du_lo, kc.dt, u_lo);
+                nu_hi = p_fma(du_hi, kc.dt, u_hi);
+            }
+            st4(io.ov + r * TX + 4 * tx, make_float4(nv_lo.x, nv_lo.y, nv_hi.x, nv_hi.y));
+            st4(io.ow + r * TX + 4 * tx, make_float4(nw_lo.x, nw_lo.y, nw_hi.x, nw_hi.y));
+            st4(io.ou + r * TX + 4 * tx, make_float4(nu_lo.x, nu_lo.y, nu_hi.x, nu_hi.y));
+            if (ACT && !DERIV && i < H) {
+                const float uo4[4] = {uc.x, uc.y, uc.z, uc.w};
+                const float un4[4] = {nu_lo.x, nu_lo.y, nu_hi.x, nu_hi.y};
+#pragma unroll
+                for (int m = 0; m < 4; ++m)
+                    if (j + m < W) record_activation(a, t, goff + m, uo4[m], un4[m]);
+            }
+            continue;
+        }
         const float *xb = sux + (r + 2) * TX + 4 * tx;
         const float4 uxc = ld4(xb);
         const float *db = sd + (r + HALO_D) * SW + HALO_U + 4 * tx;
@@ -460,18 +603,21 @@ __device__ __forceinline__ bool is_sliver(int i0, int j0, int H, int W) {
 }
 
 // Interior tiles, clamped edge tiles, or slivers (interior passes + per-cell band).
-template <bool DERIV, bool ACT, class P1>
+// PK: packed arithmetic with the launch's constants *pk (null when !PK).
+template <bool DERIV, bool ACT, bool PK = false, class P1>
 __device__ __forceinline__ void process_tile(const StepArgs &a, float t, const Stage &st,
                                              float *sux, float *suy, const TileIO &io,
-                                             unsigned active, int i0, int j0, P1 &&after_pass1) {
+                                             unsigned active, int i0, int j0, P1 &&after_pass1,
+                                             const PackConsts *pk = nullptr) {
     const int H = a.H, W = a.W;
     const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
     if (interior) {
-        compute_tile<DERIV, ACT, false>(a, t, st, sux, suy, io, active, i0, j0, after_pass1);
+        compute_tile<DERIV, ACT, false, PK>(a, pk, t, st, sux, suy, io, active, i0, j0, after_pass1);
     } else if (!is_sliver(i0, j0, H, W)) {
-        compute_tile<DERIV, ACT, true>(a, t, st, sux, suy, io, active, i0, j0, after_pass1);
+        compute_tile<DERIV, ACT, true, PK>(a, pk, t, st, sux, suy, io, active, i0, j0, after_pass1);
     } else {
-        compute_tile<DERIV, false, false>(a, t, st, sux, suy, io, active, i0, j0, after_pass1);
+        compute_tile<DERIV, false, false, PK>(a, pk, t, st, sux, suy, io, active, i0, j0,
+                                              after_pass1);
         __syncthreads();  // every cell of this tile is recomputed below where needed
         boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0,
                                      OutTile{io.ov, io.ow, io.ou, i0, j0});

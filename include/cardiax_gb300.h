@@ -73,6 +73,13 @@ const char *fk_status_string(int status);
 /* Reads (and with reset != 0 clears) the device error word of the current device. */
 int fk_device_status(int reset, int *value);
 
+/* Which kernel takes the Euler steps of every single-tissue entry point (process-wide):
+ * 0 = the tiled kernel (32 x 64-cell tiles, two passes) -- the default; 1 = the strip kernel
+ * (128-column strips walked row by row with register windows) wherever it applies (W % 128 != 1),
+ * else the tiled kernel.  Both produce the same bits; the switch exists to compare them.
+ * No counterpart in the reference. */
+int fk_select_step_kernel(int which);
+
 /* init (cardiax/solve.py:18-23): v = w = 1, u = 0 on the three planes of `state`. */
 int fk_init(fk_grid g, float *state, void *stream);
 
