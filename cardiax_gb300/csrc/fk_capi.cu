@@ -225,6 +225,7 @@ int step_once(const fk_grid &g, const float *in, float *out, const float *D, con
     a.m = m;
     for (int k = 0; k < ns; ++k) a.stim[k] = st[k];
     a.status = status;
+    a.l2_hints = l2_fits_step(g.H, g.pitch) ? 1 : 0;
     if (act && !deriv) {
         a.act_first = act->first;
         a.act_last = act->last;

@@ -100,10 +100,21 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
         return tc * TX;
     };
     int tile = blockIdx.x;
+    // L2 policies: the input state is read for the last time (the next step overwrites its
+    // buffer), D is read again by every step.  Only worth it when the live data fits in L2.
+    const bool hints = a.l2_hints != 0;
+    const uint64_t pol_dead = l2_policy_evict_first(), pol_keep = l2_policy_evict_last();
+    auto issue = [&](int tl, int s) {
+        if (hints)
+            issue_tile_hinted(tm, stage_at(smem, s), &bar[s], tile_i0(tl), tile_j0(tl), pol_dead,
+                              pol_keep);
+        else
+            issue_tile(tm, stage_at(smem, s), &bar[s], tile_i0(tl), tile_j0(tl));
+    };
     if (tid == 0)  // prologue: the first two tiles of this CTA
         for (int k = 0; k < NSTAGE - 1; ++k) {
             const int tl = tile + k * gridDim.x;
-            if (tl < ntiles) issue_tile(tm, stage_at(smem, k), &bar[k], tile_i0(tl), tile_j0(tl));
+            if (tl < ntiles) issue(tl, k);
         }
 
     unsigned active = 0;
@@ -117,9 +128,12 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
         const int ahead = tile + (NSTAGE - 1) * gridDim.x;
         if (tid == 0 && ahead < ntiles) {
             const int sa2 = (n + NSTAGE - 1) % NSTAGE;
-            issue_tile(tm, stage_at(smem, sa2), &bar[sa2], tile_i0(ahead), tile_j0(ahead));
+            issue(ahead, sa2);
         }
-        load_vw(*sa, i0, j0, io);
+        if (hints)
+            load_vw_hinted(*sa, i0, j0, io, pol_dead);
+        else
+            load_vw(*sa, i0, j0, io);
         const bool ok = mbar_wait_bounded(&bar[s], (n / NSTAGE) & 1);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) atomicOr(a.status, kStatusTimeout);
@@ -269,6 +283,22 @@ template <bool DERIV, bool ACT>
 static cudaError_t set_smem_attr() {
     return cudaFuncSetAttribute(fk_step_kernel<DERIV, ACT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_STEP_BYTES);
+}
+
+// Whether the live data of a step on an H x pitch grid (the new state and D: 4 planes) fits in
+// 3/4 of the current device's L2, so that L2 eviction hints pay off (looked up once per device).
+bool l2_fits_step(int64_t H, int64_t pitch) {
+    static thread_local int dev_cached = -1;
+    static thread_local int64_t l2_bytes = 0;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (dev != dev_cached) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, dev) != cudaSuccess) v = 0;
+        l2_bytes = v;
+        dev_cached = dev;
+    }
+    return 4 * H * pitch * (int64_t)sizeof(float) * 4 <= 3 * l2_bytes;
 }
 
 cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream) {

@@ -68,6 +68,9 @@ struct StepArgs {
     // activation tracking (upstrokes of u through `act_threshold`); null when off
     int32_t *act_first, *act_last, *act_count;
     float act_threshold;
+    // nonzero: the step's live data (the new state and D) fits in L2, so the step kernel marks
+    // the input state's reads evict-first and D's evict-last (set by the host per device)
+    int l2_hints;
 };
 
 enum : int { kStatusTimeout = 1 };
@@ -83,6 +86,8 @@ struct StepMaps {
 // above it during step t -> t+1 gets act_last = t+1, act_first = t+1 if it was -1, and
 // act_count + 1.
 cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream);
+// Whether one step's live data on an H x pitch grid fits in L2 (sets StepArgs::l2_hints).
+bool l2_fits_step(int64_t H, int64_t pitch);
 
 // ---- batched tissues ------------------------------------------------------------------------
 // Device-resident descriptors of one tissue in a batch: the step arguments and TMA maps for

@@ -216,6 +216,33 @@ __device__ __forceinline__ void issue_tile(const StepMaps &tm, const Stage &st, 
     issue_tile(&tm.u, &tm.d, st, bar, i0, j0);
 }
 
+// issue_tile with L2 policies: the input state's u (read for the last time: the next step
+// overwrites this buffer) and D (re-read every step).
+__device__ __forceinline__ void issue_tile_hinted(const StepMaps &tm, const Stage &st,
+                                                  uint64_t *bar, int i0, int j0, uint64_t pol_u,
+                                                  uint64_t pol_d) {
+    mbar_arrive_expect_tx(bar, SMEM_STAGE_BYTES);
+    tma_load_2d_hint(st.u, &tm.u, j0 - HALO_U, i0 - HALO_U, bar, pol_u);
+    tma_load_2d_hint(st.d, &tm.d, j0 - HALO_U, i0 - HALO_D, bar, pol_d);
+}
+
+// load_vw with an L2 policy (the v, w read here are read for the last time).
+__device__ __forceinline__ void load_vw_hinted(const StepArgs &a, int i0, int j0, TileIO &io,
+                                               uint64_t pol) {
+    const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
+    const int j = j0 + 4 * tx;
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+        const int i = i0 + RPT * ty + k;
+        io.v[k] = io.w[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < a.H && j < a.W) {
+            const int64_t off = (int64_t)i * a.pitch + j;
+            io.v[k] = ld_f4_hint(a.v + off, pol);
+            io.w[k] = ld_f4_hint(a.w + off, pol);
+        }
+    }
+}
+
 // This thread's v, w for pass 2 (16-byte loads, zero outside the grid).
 __device__ __forceinline__ void load_vw(const StepArgs &a, int i0, int j0, TileIO &io) {
     const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
@@ -377,6 +404,16 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const PackConsts
     // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
     const int tx = tid % NTX, ty = tid / NTX;
     const int j = j0 + 4 * tx;
+    // PK: the u_x and D rows RPT*ty-2 .. RPT*ty+RPT+1 of this thread's quad, read once for all
+    // of its rows (entry q holds row RPT*ty - 2 + q)
+    Quad uxr[PK ? RPT + 4 : 1], dxr[PK ? RPT + 4 : 1];
+    if constexpr (PK) {
+#pragma unroll
+        for (int q = 0; q < RPT + 4; ++q) {
+            uxr[q] = ld_quad(sux + (RPT * ty + q) * TX + 4 * tx);
+            dxr[q] = ld_quad(sd + (RPT * ty + q) * SW + HALO_U + 4 * tx);
+        }
+    }
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
         const int r = RPT * ty + k;
@@ -384,21 +421,22 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const PackConsts
         const int64_t goff = (int64_t)i * pitch + j;
         if constexpr (PK) {
             const PackConsts &kc = *pk;
-            const float *xb = sux + (r + 2) * TX + 4 * tx;
             const float *db = sd + (r + HALO_D) * SW + HALO_U + 4 * tx;
-            const Quad uxc = ld_quad(xb), dcq = ld_quad(db);
+            const int o = k + 2;  // window entry of row r
+            const Quad uxc = uxr[o], dcq = dxr[o];
             Quad uxx, dxD;
             if (!EDGE || (i != 0 && i != H - 1)) {
-                uxx = q_central(kc, ld_quad(xb - 2 * TX), ld_quad(xb - TX), ld_quad(xb + TX),
-                                ld_quad(xb + 2 * TX));
-                dxD = q_central(kc, ld_quad(db - 2 * SW), ld_quad(db - SW), ld_quad(db + SW),
-                                ld_quad(db + 2 * SW));
-            } else if (i == 0) {  // head rows on u_x rows 0..3 and D rows 0..3
-                uxx = q_head(kc, uxc, ld_quad(xb + TX), ld_quad(xb + 2 * TX), ld_quad(xb + 3 * TX));
-                dxD = q_head(kc, dcq, ld_quad(db + SW), ld_quad(db + 2 * SW), ld_quad(db + 3 * SW));
-            } else {  // i == H-1: tail rows on rows H-4 .. H-1
-                uxx = q_tail(kc, ld_quad(xb - 3 * TX), ld_quad(xb - 2 * TX), ld_quad(xb - TX), uxc);
-                dxD = q_tail(kc, ld_quad(db - 3 * SW), ld_quad(db - 2 * SW), ld_quad(db - SW), dcq);
+                uxx = q_central(kc, uxr[o - 2], uxr[o - 1], uxr[o + 1], uxr[o + 2]);
+                dxD = q_central(kc, dxr[o - 2], dxr[o - 1], dxr[o + 1], dxr[o + 2]);
+            } else if (k == 0 && i == 0) {  // head rows on u_x rows 0..3 and D rows 0..3
+                uxx = q_head(kc, uxr[o], uxr[o + 1], uxr[o + 2], uxr[o + 3]);
+                dxD = q_head(kc, dxr[o], dxr[o + 1], dxr[o + 2], dxr[o + 3]);
+            } else {  // i == H-1: tail rows on rows H-4 .. H-1 (row r-3 read here when k == 0)
+                const float *xb = sux + (r + 2) * TX + 4 * tx;
+                const Quad ux3 = k >= 1 ? uxr[k >= 1 ? o - 3 : 0] : ld_quad(xb - 3 * TX);
+                const Quad d3 = k >= 1 ? dxr[k >= 1 ? o - 3 : 0] : ld_quad(db - 3 * SW);
+                uxx = q_tail(kc, ux3, uxr[o - 2], uxr[o - 1], uxc);
+                dxD = q_tail(kc, d3, dxr[o - 2], dxr[o - 1], dcq);
             }
             uxx = q_scale(uxx, kc.rdx);
             dxD = q_scale(dxD, kc.rdx);
