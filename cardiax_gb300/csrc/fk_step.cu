@@ -66,13 +66,14 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
     // 128-byte aligned base, offset as a pointer so that the compiler keeps the shared-memory
     // state space (integer address arithmetic would turn every access into a generic one)
     unsigned char *smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
-    float *sux = reinterpret_cast<float *>(smem + NSTAGE * SMEM_STAGE_BYTES);  // [SUX_H][TX]
-    float *suy = sux + TX * SUX_H;                                               // [TY][SW]
+    // u_x and u_y planes, double-buffered: pass 1 of tile n+1 may start while slower warps are
+    // still in pass 2 of tile n (the new state goes straight to global memory, so the only CTA
+    // barrier of an interior tile is the one between its passes)
+    float *sux = reinterpret_cast<float *>(smem + NSTAGE * SMEM_STAGE_BYTES);  // [2][SUX_H][TX]
+    float *suy = sux + 2 * TX * SUX_H;                                           // [2][TY][SW]
     TileIO io;
-    io.ov = suy + SW * TY;                                                       // [TY][TX] x 3
-    io.ow = io.ov + TX * TY;
-    io.ou = io.ow + TX * TY;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(io.ou + TX * TY);              // [NSTAGE]
+    io.ov = io.ow = io.ou = nullptr;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(suy + 2 * SW * TY);            // [NSTAGE]
     StepArgs *sa = reinterpret_cast<StepArgs *>(bar + NSTAGE);
 
     const int tid = threadIdx.x;
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
     if (tid == 0) {
         prefetch_tensormap(&tm.u);
         prefetch_tensormap(&tm.d);
-        for (int k = 0; k < NSTAGE; ++k) mbar_init(&bar[k], 1);
+        for (int q = 0; q < NSTAGE; ++q) mbar_init(&bar[q], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -112,9 +113,9 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
             issue_tile(tm, stage_at(smem, s), &bar[s], tile_i0(tl), tile_j0(tl));
     };
     if (tid == 0)  // prologue: the first two tiles of this CTA
-        for (int k = 0; k < NSTAGE - 1; ++k) {
-            const int tl = tile + k * gridDim.x;
-            if (tl < ntiles) issue(tl, k);
+        for (int q = 0; q < NSTAGE - 1; ++q) {
+            const int tl = tile + q * gridDim.x;
+            if (tl < ntiles) issue(tl, q);
         }
 
     unsigned active = 0;
@@ -124,30 +125,24 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
     for (int n = 0; tile < ntiles; ++n, tile += gridDim.x) {
         const int s = n % NSTAGE;
         const int i0 = tile_i0(tile), j0 = tile_j0(tile);
-        // tile n+2 goes into the stage of tile n-1, which every thread has finished reading
-        const int ahead = tile + (NSTAGE - 1) * gridDim.x;
-        if (tid == 0 && ahead < ntiles) {
-            const int sa2 = (n + NSTAGE - 1) % NSTAGE;
-            issue(ahead, sa2);
-        }
         if (hints)
             load_vw_hinted(*sa, i0, j0, io, pol_dead);
         else
             load_vw(*sa, i0, j0, io);
         const bool ok = mbar_wait_bounded(&bar[s], (n / NSTAGE) & 1);
-        if (__syncthreads_or(!ok)) {
+        // after the barrier between this tile's passes every thread has finished tile n-1, so
+        // its stage takes tile n+2
+        const int ahead = tile + (NSTAGE - 1) * gridDim.x;
+        auto refill = [&] {
+            if (tid == 0 && ahead < ntiles) issue(ahead, (n + NSTAGE - 1) % NSTAGE);
+        };
+        float *ux_n = sux + (n & 1) * (TX * SUX_H), *uy_n = suy + (n & 1) * (SW * TY);
+        if (!process_tile<DERIV, ACT, true, true>(*sa, a.t, stage_at(smem, s), ux_n, uy_n, io,
+                                                  active, i0, j0, NoHook{}, &k, ok, refill)) {
             if (tid == 0) atomicOr(a.status, kStatusTimeout);
             return;
         }
-        // before pass 2 rewrites the output tiles, the stores of tile n-1 must have read them
-        auto outputs_free = [&] {
-            if (threadIdx.x == 0) bulk_wait_read();
-        };
-        process_tile<DERIV, ACT, true>(*sa, a.t, stage_at(smem, s), sux, suy, io, active, i0, j0,
-                                       outputs_free, &k);
-        store_tile(tm, io, i0, j0);  // its barrier also frees sux, suy and stage s
     }
-    if (tid == 0) bulk_wait_all();
 }
 
 // ---- batched kernel: persistent CTAs over the tiles of many tissues ------------------------
@@ -282,7 +277,7 @@ cudaError_t launch_batch_copyback(const BatchTissue *tissues, int n_tissues, cud
 template <bool DERIV, bool ACT>
 static cudaError_t set_smem_attr() {
     return cudaFuncSetAttribute(fk_step_kernel<DERIV, ACT>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_STEP_BYTES);
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_STEP_DIRECT_BYTES);
 }
 
 // Whether the live data of a step on an H x pitch grid (the new state and D: 4 planes) fits in
@@ -321,7 +316,7 @@ cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cud
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(NT);
-    cfg.dynamicSmemBytes = SMEM_STEP_BYTES;
+    cfg.dynamicSmemBytes = SMEM_STEP_DIRECT_BYTES;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;

@@ -50,6 +50,10 @@ constexpr int SMEM_PLANE_BYTES = TX * TY * 4;     // one dense output plane
 constexpr int SMEM_ARGS_BYTES = 1024;  // staged StepArgs (static_assert in fk_step.cu)
 constexpr int SMEM_STEP_BYTES = NSTAGE * SMEM_STAGE_BYTES + SMEM_UX_BYTES + SMEM_UY_BYTES +
                                 3 * SMEM_PLANE_BYTES + 8 * NSTAGE + SMEM_ARGS_BYTES + 128;
+// fk_step_kernel: no output tiles (the new state is stored from registers), u_x and u_y
+// double-buffered
+constexpr int SMEM_STEP_DIRECT_BYTES = NSTAGE * SMEM_STAGE_BYTES + 2 * (SMEM_UX_BYTES + SMEM_UY_BYTES) +
+                                       8 * NSTAGE + SMEM_ARGS_BYTES + 128;
 // Cells within this distance of an edge take the per-cell boundary path (one-sided stencils
 // and edge padding reach 4 cells in).
 constexpr int BAND = 4;

@@ -65,7 +65,8 @@ __device__ __forceinline__ void record_activation(const StepArgs &a, float t, in
     }
 }
 
-// Output tile in shared memory (dense TY x TX per plane) that the TMA stores write out.
+// Output tile in shared memory (dense TY x TX per plane) that the TMA stores write out; with
+// null planes, cells go straight to the output state (a.vo, a.wo, a.uo) in global memory.
 struct OutTile {
     float *v, *w, *u;
     int i0, j0;
@@ -113,17 +114,26 @@ __device__ __noinline__ void boundary_cell(const StepArgs &a, float t, unsigned 
         if (acc != 0.0f) r.j_ion = acc;
     }
     const float du = diffusion(d, dxD, dyD, UX(i), UY(j), uxx, uyy) + r.j_ion;
-    const int lo = (i - o.i0) * TX + (j - o.j0);
+    float ov, ow, ou;
     if (deriv) {
-        o.v[lo] = r.dv;
-        o.w[lo] = r.dw;
-        o.u[lo] = du;
+        ov = r.dv;
+        ow = r.dw;
+        ou = du;
     } else {
-        o.v[lo] = fmaf(r.dv, a.dt, v);
-        o.w[lo] = fmaf(r.dw, a.dt, w);
-        const float un = fmaf(du, a.dt, u);
-        o.u[lo] = un;
-        if (ACT) record_activation(a, t, off, u, un);
+        ov = fmaf(r.dv, a.dt, v);
+        ow = fmaf(r.dw, a.dt, w);
+        ou = fmaf(du, a.dt, u);
+        if (ACT) record_activation(a, t, off, u, ou);
+    }
+    if (o.v) {
+        const int lo = (i - o.i0) * TX + (j - o.j0);
+        o.v[lo] = ov;
+        o.w[lo] = ow;
+        o.u[lo] = ou;
+    } else {
+        __stcg(a.vo + off, ov);
+        __stcg(a.wo + off, ow);
+        __stcg(a.uo + off, ou);
     }
 }
 
@@ -293,11 +303,23 @@ static __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_ro
 // EDGE: the tile touches the grid edge (and is not a one-row or one-column sliver): the halo
 // is clamped and every derivative picks the reference's row type, exactly as the padded
 // arrays of cardiax/solve.py:29-32,49-54 do.
-template <bool DERIV, bool ACT, bool EDGE, bool PK, class P1>
-__device__ __forceinline__ void compute_tile(const StepArgs &a, const PackConsts *pk, float t,
+//
+// DIRECT (with PK): pass 2 writes the new state straight to global memory with 16-byte stores
+// instead of into output tiles for TMA stores.  The caller then needs no barrier after the tile:
+// the one barrier between the passes also votes on `ok` (this thread's wait for the tile's TMA
+// data; the tile is abandoned and false returned when any thread's wait failed) and is followed
+// by `after_barrier` (every thread has finished the previous tile by then).  band_mask: store
+// no cell within BAND of an edge (a sliver tile's band is recomputed per cell afterwards).
+struct NoHook {
+    __device__ void operator()() const {}
+};
+template <bool DERIV, bool ACT, bool EDGE, bool PK, bool DIRECT = false, class P1, class P2 = NoHook>
+__device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts *pk, float t,
                                              const Stage &st, float *sux, float *suy,
                                              const TileIO &io, unsigned active, int i0, int j0,
-                                             P1 &&after_pass1) {
+                                             P1 &&after_pass1, bool ok = true,
+                                             P2 &&after_barrier = P2{}, bool band_mask = false) {
+    static_assert(!DIRECT || PK, "direct stores are implemented on the packed path");
     const int tid = threadIdx.x;
     const int H = a.H, W = a.W, pitch = a.pitch;
     const float rdx = a.rdx;
@@ -306,6 +328,8 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const PackConsts
     if (EDGE) {
         clamp_halo(su, SU_H, HALO_U, i0, j0, H, W);
         clamp_halo(sd, SD_H, HALO_D, i0, j0, H, W);
+        // the stage is refilled by TMA later: order these generic writes before that
+        if (DIRECT) fence_async_smem();
         __syncthreads();
     }
 
@@ -399,7 +423,12 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const PackConsts
         suy[r * SW + c] = o * rdx;
     }
     after_pass1();  // every thread (the hook picks its warps): free the output tiles, start loads
-    __syncthreads();
+    if constexpr (DIRECT) {
+        if (__syncthreads_or(!ok)) return false;
+        after_barrier();
+    } else {
+        __syncthreads();
+    }
 
     // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
     const int tx = tid % NTX, ty = tid / NTX;
@@ -521,15 +550,44 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const PackConsts
                 nu_lo = p_fma(du_lo, kc.dt, u_lo);
                 nu_hi = p_fma(du_hi, kc.dt, u_hi);
             }
-            st4(io.ov + r * TX + 4 * tx, make_float4(nv_lo.x, nv_lo.y, nv_hi.x, nv_hi.y));
-            st4(io.ow + r * TX + 4 * tx, make_float4(nw_lo.x, nw_lo.y, nw_hi.x, nw_hi.y));
-            st4(io.ou + r * TX + 4 * tx, make_float4(nu_lo.x, nu_lo.y, nu_hi.x, nu_hi.y));
+            const float4 ov4 = make_float4(nv_lo.x, nv_lo.y, nv_hi.x, nv_hi.y);
+            const float4 ow4 = make_float4(nw_lo.x, nw_lo.y, nw_hi.x, nw_hi.y);
+            const float4 ou4 = make_float4(nu_lo.x, nu_lo.y, nu_hi.x, nu_hi.y);
+            // a cell this tile stores: inside the grid, and outside the band when masked
+            auto stored = [&](int jj) {
+                return jj < W && !(band_mask && (i < BAND || i >= H - BAND || jj < BAND ||
+                                                 jj >= W - BAND));
+            };
+            if constexpr (DIRECT) {
+                if (i < H && j < W) {
+                    if (!band_mask && j + 3 < W) {
+                        __stcg(reinterpret_cast<float4 *>(a.vo + goff), ov4);
+                        __stcg(reinterpret_cast<float4 *>(a.wo + goff), ow4);
+                        __stcg(reinterpret_cast<float4 *>(a.uo + goff), ou4);
+                    } else {
+                        const float fv[4] = {ov4.x, ov4.y, ov4.z, ov4.w};
+                        const float fw[4] = {ow4.x, ow4.y, ow4.z, ow4.w};
+                        const float fu[4] = {ou4.x, ou4.y, ou4.z, ou4.w};
+#pragma unroll
+                        for (int m = 0; m < 4; ++m)
+                            if (stored(j + m)) {
+                                __stcg(a.vo + goff + m, fv[m]);
+                                __stcg(a.wo + goff + m, fw[m]);
+                                __stcg(a.uo + goff + m, fu[m]);
+                            }
+                    }
+                }
+            } else {
+                st4(io.ov + r * TX + 4 * tx, ov4);
+                st4(io.ow + r * TX + 4 * tx, ow4);
+                st4(io.ou + r * TX + 4 * tx, ou4);
+            }
             if (ACT && !DERIV && i < H) {
                 const float uo4[4] = {uc.x, uc.y, uc.z, uc.w};
-                const float un4[4] = {nu_lo.x, nu_lo.y, nu_hi.x, nu_hi.y};
+                const float un4[4] = {ou4.x, ou4.y, ou4.z, ou4.w};
 #pragma unroll
                 for (int m = 0; m < 4; ++m)
-                    if (j + m < W) record_activation(a, t, goff + m, uo4[m], un4[m]);
+                    if (stored(j + m)) record_activation(a, t, goff + m, uo4[m], un4[m]);
             }
             continue;
         }
@@ -632,6 +690,7 @@ __device__ __forceinline__ void compute_tile(const StepArgs &a, const PackConsts
                 if (j + m < W) record_activation(a, t, goff + m, uu[m], ou[m]);
         }
     }
+    return true;
 }
 
 // A tile that needs the per-cell boundary path: the last row or column of tiles holds a
@@ -642,17 +701,29 @@ __device__ __forceinline__ bool is_sliver(int i0, int j0, int H, int W) {
 
 // Interior tiles, clamped edge tiles, or slivers (interior passes + per-cell band).
 // PK: packed arithmetic with the launch's constants *pk (null when !PK).
-template <bool DERIV, bool ACT, bool PK = false, class P1>
-__device__ __forceinline__ void process_tile(const StepArgs &a, float t, const Stage &st,
+// DIRECT: see compute_tile; returns false when the tile was abandoned (a failed TMA wait).
+template <bool DERIV, bool ACT, bool PK = false, bool DIRECT = false, class P1, class P2 = NoHook>
+__device__ __forceinline__ bool process_tile(const StepArgs &a, float t, const Stage &st,
                                              float *sux, float *suy, const TileIO &io,
                                              unsigned active, int i0, int j0, P1 &&after_pass1,
-                                             const PackConsts *pk = nullptr) {
+                                             const PackConsts *pk = nullptr, bool ok = true,
+                                             P2 &&after_barrier = P2{}) {
     const int H = a.H, W = a.W;
     const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
     if (interior) {
-        compute_tile<DERIV, ACT, false, PK>(a, pk, t, st, sux, suy, io, active, i0, j0, after_pass1);
+        return compute_tile<DERIV, ACT, false, PK, DIRECT>(a, pk, t, st, sux, suy, io, active, i0,
+                                                           j0, after_pass1, ok, after_barrier);
     } else if (!is_sliver(i0, j0, H, W)) {
-        compute_tile<DERIV, ACT, true, PK>(a, pk, t, st, sux, suy, io, active, i0, j0, after_pass1);
+        return compute_tile<DERIV, ACT, true, PK, DIRECT>(a, pk, t, st, sux, suy, io, active, i0,
+                                                          j0, after_pass1, ok, after_barrier);
+    } else if (DIRECT) {
+        // interior cells from the tile passes; the band cells per cell, straight to global memory
+        if (!compute_tile<DERIV, ACT, false, PK, DIRECT>(a, pk, t, st, sux, suy, io, active, i0,
+                                                         j0, after_pass1, ok, after_barrier, true))
+            return false;
+        boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0,
+                                     OutTile{nullptr, nullptr, nullptr, i0, j0});
+        return true;
     } else {
         compute_tile<DERIV, false, false, PK>(a, pk, t, st, sux, suy, io, active, i0, j0,
                                               after_pass1);
@@ -669,6 +740,7 @@ __device__ __forceinline__ void process_tile(const StepArgs &a, float t, const S
                                       io.ou[idx]);
             }
         }
+        return true;
     }
 }
 
