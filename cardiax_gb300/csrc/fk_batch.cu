@@ -181,12 +181,19 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
             return rc;
         }
     }
-    for (int k : order) {
-        const fk_grid &g = tissues[k].g;
-        for (int64_t i0 = 0; i0 < g.H; i0 += TY)
-            for (int64_t j0 = 0; j0 < g.W; j0 += TX)
-                b->h_items.push_back(BatchItem{k, (int32_t)i0, (int32_t)j0, 0});
-    }
+    // work list: the edge tiles of every tissue (the costlier clamped-halo path) first, then the
+    // interior tiles, each group with the larger tissues first
+    for (int pass = 0; pass < 2; ++pass)
+        for (int k : order) {
+            const fk_grid &g = tissues[k].g;
+            for (int64_t i0 = 0; i0 < g.H; i0 += TY)
+                for (int64_t j0 = 0; j0 < g.W; j0 += TX) {
+                    const bool interior = i0 >= BAND && i0 + TY <= g.H - BAND && j0 >= BAND &&
+                                          j0 + TX <= g.W - BAND;
+                    if (interior == (pass == 1))
+                        b->h_items.push_back(BatchItem{k, (int32_t)i0, (int32_t)j0, 0});
+                }
+        }
     cudaStream_t s = (cudaStream_t)stream;
     if (cudaMemcpyAsync(b->d_maps, b->h_maps.data(), sizeof(BatchMaps) * n,
                         cudaMemcpyHostToDevice, s) != cudaSuccess ||

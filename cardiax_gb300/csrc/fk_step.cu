@@ -153,18 +153,19 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
                     int t_offset, int parity, int *status) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
-    float *sux = reinterpret_cast<float *>(smem + NSTAGE * SMEM_STAGE_BYTES);
-    float *suy = sux + TX * SUX_H;
+    // as fk_step_kernel: u_x / u_y double-buffered, new state stored from registers; and the
+    // tissue arguments double-buffered too (item n stages its tissue's arguments while slower
+    // warps may still be in pass 2 of item n-1)
+    float *sux = reinterpret_cast<float *>(smem + NSTAGE * SMEM_STAGE_BYTES);  // [2][SUX_H][TX]
+    float *suy = sux + 2 * TX * SUX_H;                                           // [2][TY][SW]
     TileIO io;
-    io.ov = suy + SW * TY;
-    io.ow = io.ov + TX * TY;
-    io.ou = io.ow + TX * TY;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(io.ou + TX * TY);
-    StepArgs *sa = reinterpret_cast<StepArgs *>(bar + NSTAGE);  // the current tile's tissue
+    io.ov = io.ow = io.ou = nullptr;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(suy + 2 * SW * TY);            // [NSTAGE]
+    unsigned char *args = reinterpret_cast<unsigned char *>(bar + NSTAGE);       // [2] StepArgs
 
     const int tid = threadIdx.x;
     if (tid == 0) {
-        for (int k = 0; k < NSTAGE; ++k) mbar_init(&bar[k], 1);
+        for (int q = 0; q < NSTAGE; ++q) mbar_init(&bar[q], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -172,43 +173,38 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
     grid_launch_dependents();
     const float t = (float)(*t_dev + t_offset);
     int it = blockIdx.x;
+    auto issue = [&](int x, int st) {
+        const BatchItem b = items[x];
+        issue_tile(maps[b.tissue].maps[parity], stage_at(smem, st), &bar[st], b.i0, b.j0);
+    };
     if (tid == 0)
-        for (int k = 0; k < NSTAGE - 1; ++k) {
-            const int x = it + k * gridDim.x;
-            if (x < n_items) {
-                const BatchItem b = items[x];
-                issue_tile(maps[b.tissue].maps[parity], stage_at(smem, k), &bar[k], b.i0, b.j0);
-            }
+        for (int q = 0; q < NSTAGE - 1; ++q) {
+            const int x = it + q * gridDim.x;
+            if (x < n_items) issue(x, q);
         }
     for (int n = 0; it < n_items; ++n, it += gridDim.x) {
         const int s = n % NSTAGE;
-        const int ahead = it + (NSTAGE - 1) * gridDim.x;
-        if (tid == 0 && ahead < n_items) {
-            const BatchItem b = items[ahead];
-            const int sa2 = (n + NSTAGE - 1) % NSTAGE;
-            issue_tile(maps[b.tissue].maps[parity], stage_at(smem, sa2), &bar[sa2], b.i0, b.j0);
-        }
         const BatchItem b = items[it];
+        StepArgs *sa = reinterpret_cast<StepArgs *>(args + (n & 1) * SMEM_ARGS_BYTES);
         stage_args(sa, &tissues[b.tissue].args[parity]);  // this tissue's arguments
         __syncthreads();
         load_vw(*sa, b.i0, b.j0, io);
         const bool ok = mbar_wait_bounded(&bar[s], (n / NSTAGE) & 1);
-        if (__syncthreads_or(!ok)) {
+        unsigned active = 0;
+        for (int q = 0; q < sa->n_stim; ++q)
+            if (stim_active(sa->stim[q], t)) active |= 1u << q;
+        const int ahead = it + (NSTAGE - 1) * gridDim.x;
+        auto refill = [&] {  // after the pass barrier: item n-1 is done, its stage is free
+            if (tid == 0 && ahead < n_items) issue(ahead, (n + NSTAGE - 1) % NSTAGE);
+        };
+        float *ux_n = sux + (n & 1) * (TX * SUX_H), *uy_n = suy + (n & 1) * (SW * TY);
+        if (!process_tile<false, ACT, false, true>(*sa, t, stage_at(smem, s), ux_n, uy_n, io,
+                                                   active, b.i0, b.j0, NoHook{}, nullptr, ok,
+                                                   refill)) {
             if (tid == 0) atomicOr(status, kStatusTimeout);
             return;
         }
-        unsigned active = 0;
-        for (int k = 0; k < sa->n_stim; ++k)
-            if (stim_active(sa->stim[k], t)) active |= 1u << k;
-        auto outputs_free = [&] {
-            if (threadIdx.x == 0) bulk_wait_read();
-        };
-        process_tile<false, ACT>(*sa, t, stage_at(smem, s), sux, suy, io, active, b.i0, b.j0,
-                                 outputs_free);
-        store_tile(maps[b.tissue].maps[parity], io, b.i0, b.j0);
-        __syncthreads();  // the staged arguments are rewritten for the next item
     }
-    if (tid == 0) bulk_wait_all();
 }
 
 __global__ void add_int_kernel(int *p, int v) { *p += v; }

@@ -107,7 +107,7 @@ struct BatchItem {
     int32_t tissue, i0, j0, pad;
 };
 
-constexpr int SMEM_BATCH_BYTES = SMEM_STEP_BYTES;
+constexpr int SMEM_BATCH_BYTES = SMEM_STEP_DIRECT_BYTES + SMEM_ARGS_BYTES;  // two argument slots
 
 // One Euler step of every tissue: persistent CTAs drain `items`; the step index is
 // *t_dev + t_offset (so that a captured graph can be replayed for successive steps).

@@ -304,7 +304,7 @@ static __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_ro
 // is clamped and every derivative picks the reference's row type, exactly as the padded
 // arrays of cardiax/solve.py:29-32,49-54 do.
 //
-// DIRECT (with PK): pass 2 writes the new state straight to global memory with 16-byte stores
+// DIRECT: pass 2 writes the new state straight to global memory with 16-byte stores
 // instead of into output tiles for TMA stores.  The caller then needs no barrier after the tile:
 // the one barrier between the passes also votes on `ok` (this thread's wait for the tile's TMA
 // data; the tile is abandoned and false returned when any thread's wait failed) and is followed
@@ -319,7 +319,6 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                                              const TileIO &io, unsigned active, int i0, int j0,
                                              P1 &&after_pass1, bool ok = true,
                                              P2 &&after_barrier = P2{}, bool band_mask = false) {
-    static_assert(!DIRECT || PK, "direct stores are implemented on the packed path");
     const int tid = threadIdx.x;
     const int H = a.H, W = a.W, pitch = a.pitch;
     const float rdx = a.rdx;
@@ -681,13 +680,35 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                 ou[m] = fmaf(du, a.dt, uu[m]);
             }
         }
-        st4(io.ov + r * TX + 4 * tx, make_float4(ov[0], ov[1], ov[2], ov[3]));
-        st4(io.ow + r * TX + 4 * tx, make_float4(ow[0], ow[1], ow[2], ow[3]));
-        st4(io.ou + r * TX + 4 * tx, make_float4(ou[0], ou[1], ou[2], ou[3]));
+        auto stored = [&](int jj) {
+            return jj < W && !(band_mask && (i < BAND || i >= H - BAND || jj < BAND ||
+                                             jj >= W - BAND));
+        };
+        if constexpr (DIRECT) {
+            if (i < H && j < W) {
+                if (!band_mask && j + 3 < W) {
+                    __stcg(reinterpret_cast<float4 *>(a.vo + goff), make_float4(ov[0], ov[1], ov[2], ov[3]));
+                    __stcg(reinterpret_cast<float4 *>(a.wo + goff), make_float4(ow[0], ow[1], ow[2], ow[3]));
+                    __stcg(reinterpret_cast<float4 *>(a.uo + goff), make_float4(ou[0], ou[1], ou[2], ou[3]));
+                } else {
+#pragma unroll
+                    for (int m = 0; m < 4; ++m)
+                        if (stored(j + m)) {
+                            __stcg(a.vo + goff + m, ov[m]);
+                            __stcg(a.wo + goff + m, ow[m]);
+                            __stcg(a.uo + goff + m, ou[m]);
+                        }
+                }
+            }
+        } else {
+            st4(io.ov + r * TX + 4 * tx, make_float4(ov[0], ov[1], ov[2], ov[3]));
+            st4(io.ow + r * TX + 4 * tx, make_float4(ow[0], ow[1], ow[2], ow[3]));
+            st4(io.ou + r * TX + 4 * tx, make_float4(ou[0], ou[1], ou[2], ou[3]));
+        }
         if (ACT && !DERIV && i < H) {
 #pragma unroll
             for (int m = 0; m < 4; ++m)
-                if (j + m < W) record_activation(a, t, goff + m, uu[m], ou[m]);
+                if (stored(j + m)) record_activation(a, t, goff + m, uu[m], ou[m]);
         }
     }
     return true;
