@@ -270,32 +270,38 @@ __device__ __forceinline__ void load_vw(const StepArgs &a, int i0, int j0, TileI
 }
 
 // Edge tiles: replace the zero fill of the out-of-grid halo by the reference's edge padding
-// (copies of the first/last row and column).  Only the 4 grid rows and columns beyond each edge
-// are rewritten: the stencils of in-grid cells read at most 2 beyond (u_x, u_y and D at rows /
-// columns -2 .. H+1 / W+1), and what is computed for out-of-grid cells is never stored.
+// (jnp.pad(..., "edge")): a cell at grid row x, column y outside the grid takes the value of
+// (clamp(x, 0, H-1), clamp(y, 0, W-1)).  Only the 4 rows and columns beyond each edge are
+// rewritten: the stencils of in-grid cells read at most 2 beyond (u_x, u_y and D at rows /
+// columns -2 .. H+1 / W+1), and what is computed for out-of-grid cells is never stored.  Every
+// source cell is inside the grid, hence never a target: one pass, no barrier inside.
+// Buffer row b holds grid row i0 - halo_rows + b, buffer column c grid column j0 - HALO_U + c.
 static __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_rows, int i0, int j0,
                                                int H, int W) {
-    constexpr int SW4 = SW / 4;  // float4 per buffer row (rows are 16-byte aligned)
-    const int tid = threadIdx.x;
-    // rows -4 .. -1 take row 0, rows H .. H+3 take row H-1 (where they fall in the buffer)
-    for (int it = tid; it < 8 * SW4; it += NT) {
-        const int k = it / SW4, c4 = it % SW4;
-        const int gr = k < 4 ? k - 4 : H + (k - 4);
-        const int sr = gr - i0 + halo_rows;
-        if (sr < 0 || sr >= rows) continue;
-        const int src = (k < 4 ? 0 : H - 1) - i0 + halo_rows;
-        reinterpret_cast<float4 *>(buf + sr * SW)[c4] =
-            reinterpret_cast<const float4 *>(buf + src * SW)[c4];
-    }
-    __syncthreads();
-    // then columns -4 .. -1 and W .. W+3 (corners get the corner cell)
-    for (int it = tid; it < 8 * rows; it += NT) {
-        const int k = it & 7, sr = it >> 3;
-        const int gc = k < 4 ? k - 4 : W + (k - 4);
-        const int c = gc - j0 + HALO_U;
-        if (c < 0 || c >= SW) continue;
-        const int src = (k < 4 ? 0 : W - 1) - j0 + HALO_U;
-        buf[sr * SW + c] = buf[sr * SW + src];
+    const int base_r = i0 - halo_rows, base_c = j0 - HALO_U;
+    // band rows: grid rows -4 .. -1 and H .. H+3 inside the buffer; then the in-grid rows
+    const int t_lo = max(0, -4 - base_r), t_hi = min(rows, -base_r);
+    const int b_lo = max(0, H - base_r), b_hi = min(rows, H + 4 - base_r);
+    const int nt = max(0, t_hi - t_lo), nb = max(0, b_hi - b_lo);
+    const int g_lo = max(0, -base_r), g_hi = min(rows, H - base_r);
+    // band columns of the in-grid rows: grid columns -4 .. -1 and W .. W+3 (8 candidates per
+    // row, those outside the buffer skipped)
+    const int n_rows = (nt + nb) * SW, n_cols = max(0, g_hi - g_lo) * 8;
+    for (int it = threadIdx.x; it < n_rows + n_cols; it += NT) {
+        int b, c;
+        if (it < n_rows) {  // whole band rows (corners included)
+            const int rr = it / SW;
+            c = it - rr * SW;
+            b = rr < nt ? t_lo + rr : b_lo + (rr - nt);
+        } else {
+            const int k = it - n_rows, kk = k & 7;
+            b = g_lo + (k >> 3);
+            c = (kk < 4 ? kk - 4 : W + (kk - 4)) - base_c;
+            if (c < 0 || c >= SW) continue;
+        }
+        const int sb = clampi(base_r + b, 0, H - 1) - base_r;
+        const int sc = clampi(base_c + c, 0, W - 1) - base_c;
+        buf[b * SW + c] = buf[sb * SW + sc];
     }
 }
 
@@ -381,29 +387,31 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
         const float4 x0 = ld4(b), x1 = ld4(b + 4), x2 = ld4(b + 8);
         const float e[12] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w,
                              x2.x, x2.y, x2.z, x2.w};
-        if constexpr (PK && !EDGE) {
+        // every quad takes the central rows; in an edge tile the elements at columns 0, W-1
+        // and W are then recomputed with the one-sided rows (few threads, short)
+        const int y0 = j0 + 4 * q;
+        float o[4];
+        if constexpr (PK) {
             const PackConsts &kc = *pk;  // u_y at columns c .. c+3 as the pairs (c, c+1), (c+2, c+3)
             const float2 lo = p_mul(pg_central(kc, mk2(e[2], e[3]), mk2(e[3], e[4]),
                                                mk2(e[5], e[6]), mk2(e[6], e[7])), kc.rdx);
             const float2 hi = p_mul(pg_central(kc, mk2(e[4], e[5]), mk2(e[5], e[6]),
                                                mk2(e[7], e[8]), mk2(e[8], e[9])), kc.rdx);
-            st4(suy + r * SW + HALO_U + 4 * q, make_float4(lo.x, lo.y, hi.x, hi.y));
+            o[0] = lo.x;
+            o[1] = lo.y;
+            o[2] = hi.x;
+            o[3] = hi.y;
         } else {
-            float o[4];
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                if (!EDGE) {
-                    o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
-                } else {  // u_y at padded position y: head / tail / central row of the padded line
-                    const int y = j0 + 4 * q + m;
-                    if (y <= 0) o[m] = g_head(e[m + 4], e[m + 5], e[m + 6], e[m + 7]);
-                    else if (y >= W - 1) o[m] = g_tail(e[m + 1], e[m + 2], e[m + 3], e[m + 4]);
-                    else o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]);
-                }
-            }
-            st4(suy + r * SW + HALO_U + 4 * q,
-                make_float4(o[0] * rdx, o[1] * rdx, o[2] * rdx, o[3] * rdx));
+            for (int m = 0; m < 4; ++m) o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]) * rdx;
         }
+        if (EDGE) {
+            if (y0 == 0) o[0] = g_head(e[4], e[5], e[6], e[7]) * rdx;  // column 0
+#pragma unroll
+            for (int m = 0; m < 4; ++m)  // columns W-1 and W
+                if (y0 + m == W - 1 || y0 + m == W) o[m] = g_tail(e[m + 1], e[m + 2], e[m + 3], e[m + 4]) * rdx;
+        }
+        st4(suy + r * SW + HALO_U + 4 * q, make_float4(o[0], o[1], o[2], o[3]));
     }
     if (tid >= NT - TY * 4) {  // the 2 + 2 halo columns of u_y (threads with one ux item less)
         const int h = tid - (NT - TY * 4);
@@ -477,35 +485,28 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                                  y2.x, y2.y, y2.z, y2.w};  // u_y at columns j-4 .. j+7
             const float g[12] = {dl.x, dl.y, dl.z, dl.w, dcq.lo.x, dcq.lo.y, dcq.hi.x, dcq.hi.y,
                                  dr.x, dr.y, dr.z, dr.w};  // D at columns j-4 .. j+7
-            float2 uyy_lo, uyy_hi, dyD_lo, dyD_hi;
-            if (!EDGE) {
-                uyy_lo = p_mul(pg_central(kc, mk2(f[2], f[3]), mk2(f[3], f[4]), mk2(f[5], f[6]),
-                                          mk2(f[6], f[7])), kc.rdx);
-                uyy_hi = p_mul(pg_central(kc, mk2(f[4], f[5]), mk2(f[5], f[6]), mk2(f[7], f[8]),
-                                          mk2(f[8], f[9])), kc.rdx);
-                dyD_lo = p_mul(pg_central(kc, mk2(g[2], g[3]), mk2(g[3], g[4]), mk2(g[5], g[6]),
-                                          mk2(g[6], g[7])), kc.rdx);
-                dyD_hi = p_mul(pg_central(kc, mk2(g[4], g[5]), mk2(g[5], g[6]), mk2(g[7], g[8]),
-                                          mk2(g[8], g[9])), kc.rdx);
-            } else {  // second derivative / D_y at column y: head at 0, tail at W-1
-                float uy4[4], dy4[4];
-#pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    const int y = j + m;
-                    float uyy, dyD;
-                    if (y == 0) {
-                        uyy = g_head(f[m + 4], f[m + 5], f[m + 6], f[m + 7]);
-                        dyD = g_head(g[m + 4], g[m + 5], g[m + 6], g[m + 7]);
-                    } else if (y == W - 1) {
-                        uyy = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]);
-                        dyD = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]);
-                    } else {
-                        uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
-                        dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
-                    }
-                    uy4[m] = uyy * rdx;
-                    dy4[m] = dyD * rdx;
+            float2 uyy_lo = p_mul(pg_central(kc, mk2(f[2], f[3]), mk2(f[3], f[4]), mk2(f[5], f[6]),
+                                             mk2(f[6], f[7])), kc.rdx);
+            float2 uyy_hi = p_mul(pg_central(kc, mk2(f[4], f[5]), mk2(f[5], f[6]), mk2(f[7], f[8]),
+                                             mk2(f[8], f[9])), kc.rdx);
+            float2 dyD_lo = p_mul(pg_central(kc, mk2(g[2], g[3]), mk2(g[3], g[4]), mk2(g[5], g[6]),
+                                             mk2(g[6], g[7])), kc.rdx);
+            float2 dyD_hi = p_mul(pg_central(kc, mk2(g[4], g[5]), mk2(g[5], g[6]), mk2(g[7], g[8]),
+                                             mk2(g[8], g[9])), kc.rdx);
+            if (EDGE && (j == 0 || (j <= W - 1 && W - 1 <= j + 3))) {
+                // the one-sided rows at column 0 (head) and W-1 (tail), second derivative / D_y
+                float uy4[4] = {uyy_lo.x, uyy_lo.y, uyy_hi.x, uyy_hi.y};
+                float dy4[4] = {dyD_lo.x, dyD_lo.y, dyD_hi.x, dyD_hi.y};
+                if (j == 0) {
+                    uy4[0] = g_head(f[4], f[5], f[6], f[7]) * rdx;
+                    dy4[0] = g_head(g[4], g[5], g[6], g[7]) * rdx;
                 }
+#pragma unroll
+                for (int m = 0; m < 4; ++m)
+                    if (j + m == W - 1) {
+                        uy4[m] = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]) * rdx;
+                        dy4[m] = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]) * rdx;
+                    }
                 uyy_lo = mk2(uy4[0], uy4[1]);
                 uyy_hi = mk2(uy4[2], uy4[3]);
                 dyD_lo = mk2(dy4[0], dy4[1]);
@@ -650,11 +651,9 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
         }
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            float uyy, dyD;
-            if (!EDGE) {
-                uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
-                dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
-            } else {  // second derivative / D_y at column y: head at 0, tail at W-1
+            float uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
+            float dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
+            if (EDGE) {  // the one-sided rows at column 0 (head) and W-1 (tail)
                 const int y = j + m;
                 if (y == 0) {
                     uyy = g_head(f[m + 4], f[m + 5], f[m + 6], f[m + 7]);
@@ -662,9 +661,6 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                 } else if (y == W - 1) {
                     uyy = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]);
                     dyD = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]);
-                } else {
-                    uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
-                    dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
                 }
             }
             uyy *= rdx;
