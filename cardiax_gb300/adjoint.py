@@ -14,14 +14,13 @@ from __future__ import annotations
 
 import ctypes
 import math
-import os
-from concurrent.futures import ThreadPoolExecutor
 from typing import Sequence
 
 import torch
 
 from . import _native as N
-from .tissue import Tissue, as_cuda_f32, stream_handle
+from .tissue import (Tissue, as_cuda_f32, params_struct, pitch_of, stimulus_table, stream_handle,
+                     to_pitched)
 
 N_THETA = 13
 
@@ -50,6 +49,19 @@ def _lib():
                                        ctypes.POINTER(ctypes.c_int64),
                                        ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.fk_adjoint_batch_workspace_bytes.restype = ctypes.c_size_t
+        L.fk_adjoint_batch_workspace_bytes.argtypes = [ctypes.c_int]
+        L.fk_batch_recompute.restype = ctypes.c_int
+        L.fk_batch_recompute.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                         ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+        L.fk_adjoint_batch_range.restype = ctypes.c_int
+        L.fk_adjoint_batch_range.argtypes = [
+            ctypes.c_int, N.Grid, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+            ctypes.c_void_p, ctypes.POINTER(N.Params),
+            ctypes.POINTER(ctypes.POINTER(N.Stimulus)), ctypes.POINTER(ctypes.c_int),
+            ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+            ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
         L._adjoint_bound = True
     return L
 
@@ -206,21 +218,59 @@ def rollout(v0, w0, u0, D, theta, stimuli, t0: int, t1: int, obs_times: Sequence
                           int(t1), list(obs_times), float(dt), float(dx), seg)
 
 
-def _per_experiment(fn, n: int):
-    """Runs fn(b) for b in 0..n-1 from a pool of host threads.  Each experiment's steps are
-    C loops that release the GIL, so the experiments' launches are issued in parallel (one
-    thread issuing thousands of small launches is what bounds a batch of small tissues)."""
-    workers = max(1, min(n, os.cpu_count() or 1))
-    if workers == 1:
-        return [fn(b) for b in range(n)]
-    with ThreadPoolExecutor(workers) as ex:
-        return list(ex.map(fn, range(n)))
+class _BatchPlan:
+    """B experiments on one grid sharing D and the parameters, as one fk_batch plan (their
+    forward steps and recomputed segments are one launch per step for all of them)."""
+
+    def __init__(self, states0, Dp, params, stimuli, dt, dx):
+        B, _, H, W = states0.shape
+        dev = states0.device
+        self.B, self.H, self.W, self.pitch = B, H, W, pitch_of(W)
+        self.grid = N.Grid(H, W, self.pitch)
+        self.params = params_struct(params)
+        self.dt, self.dx = float(dt), float(dx)
+        self.D = Dp
+        self.S = torch.zeros((B, 3, H, self.pitch), dtype=torch.float32, device=dev)
+        self.S[..., :W] = states0
+        self.scratch = torch.empty_like(self.S)
+        self.stims, self.keep = [], []
+        descs = (N.TissueDesc * B)()
+        none = N.Activation(None, None, None, 0.0)
+        for b in range(B):
+            arr, n, keep = stimulus_table(stimuli[b], H, W, self.pitch, dev)
+            self.stims.append((arr, n))
+            self.keep.append(keep)
+            descs[b] = N.TissueDesc(self.grid, self.S[b].data_ptr(), self.scratch[b].data_ptr(),
+                                    Dp.data_ptr(), self.params, arr, n, self.dt, self.dx, none)
+        self._descs = descs
+        L = N.lib()
+        nbytes = L.fk_batch_workspace_bytes(descs, B)
+        self.workspace = torch.empty(nbytes + 128, dtype=torch.uint8, device=dev)
+        base = (self.workspace.data_ptr() + 127) // 128 * 128
+        plan = ctypes.c_void_p()
+        N.call("fk_batch_create", descs, B, base, nbytes, stream_handle(), ctypes.byref(plan))
+        self.plan = plan
+
+    def advance(self, t0: int, t1: int):
+        N.call("fk_batch_forward_euler", self.plan, int(t0), int(t1), 0, stream_handle())
+
+    def close(self):
+        if getattr(self, "plan", None):
+            N.lib().fk_batch_destroy(self.plan)
+            self.plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class _RolloutBatch(torch.autograd.Function):
-    """States at ``obs_times`` of B tissues sharing D and theta (one stimulus list per tissue);
-    each tissue's forward and backward run on its own CUDA stream, issued from its own host
-    thread, so the GPU overlaps them."""
+    """States at ``obs_times`` of B tissues sharing D and theta (one stimulus list per tissue).
+    Forward, segment recomputation and the adjoint are each one launch per step for all B
+    tissues (fk_batch_forward_euler, fk_batch_recompute, fk_adjoint_batch_range), with
+    checkpoints every ``seg`` steps as in :func:`rollout`."""
 
     @staticmethod
     def forward(ctx, states0, D, theta, Cm, stimuli, t0, t1, obs_times, dt, dx, seg):
@@ -229,65 +279,85 @@ class _RolloutBatch(torch.autograd.Function):
         dev = states0.device
         t_end = max([t0] + [int(t) for t in obs_times])
         seg = seg or default_segment(t_end - t0)
+        Dp = to_pitched(D.detach(), H, W, pitch_of(W), dev)
+        bp = _BatchPlan(states0.detach(), Dp, params, stimuli, dt, dx)
         out = torch.empty((B, len(obs_times), 3, H, W), dtype=torch.float32, device=dev)
-        main = torch.cuda.current_stream(dev)
-        streams = [torch.cuda.Stream(dev) for _ in range(B)]
-        Dd = D.detach()
-
-        def one(b):
-            streams[b].wait_stream(main)
-            with torch.cuda.device(dev), torch.cuda.stream(streams[b]):
-                tis = Tissue((H, W), params, Dd, stimuli[b], dt=dt, dx=dx, device=dev)
-                tis.set_state(states0[b].detach())
-                s0 = tis.state.clone()
-                ck, snaps = forward_checkpoints(tis, s0, t0, t_end, seg, stops=list(obs_times))
-                for k, t in enumerate(obs_times):
-                    out[b, k] = snaps[int(t)]
-            return tis, ck, s0
-
-        res = _per_experiment(one, B)
-        for s in streams:
-            main.wait_stream(s)
-        ctx.tissues = [r[0] for r in res]
-        ctx.ckpts = [r[1] for r in res]
-        ctx.state0s = [r[2] for r in res]
-        ctx.streams = streams
-        ctx.t0, ctx.t1, ctx.obs_times, ctx.seg, ctx.W = t0, t_end, list(obs_times), seg, W
+        obs_at = {}
+        for k, t in enumerate(obs_times):
+            obs_at.setdefault(int(t), []).append(k)
+        marks = sorted(set(range(t0, t_end, seg)) | set(obs_at))
+        ckpts, cur = [], t0
+        for m in marks:
+            if m > cur:
+                bp.advance(cur, m)
+                cur = m
+            if (m - t0) % seg == 0 and m < t_end:
+                ckpts.append((m, bp.S.clone()))
+            for k in obs_at.get(m, []):
+                out[:, k] = bp.S[..., :W]
+        if t_end > cur:
+            bp.advance(cur, t_end)
+            for k in obs_at.get(t_end, []):
+                out[:, k] = bp.S[..., :W]
+        ctx.bp, ctx.ckpts = bp, ckpts
+        ctx.t0, ctx.t1, ctx.obs_times, ctx.seg = t0, t_end, list(obs_times), seg
         return out
 
     @staticmethod
     def backward(ctx, grad_out):
-        W = ctx.W
-        main = torch.cuda.current_stream()
-        B = len(ctx.tissues)
-        grad_out = grad_out.contiguous()
-
-        def one(b):
-            s = ctx.streams[b]
-            s.wait_stream(main)
-            tis = ctx.tissues[b]
-            with torch.cuda.device(tis.device), torch.cuda.stream(s):
-                adj = Adjoint(tis)
-                g = torch.zeros((len(ctx.obs_times),) + tuple(ctx.state0s[b].shape),
-                                dtype=torch.float32, device=tis.device)
-                g[..., :W] = grad_out[b].to(torch.float32)
-                lam0 = adj.rollout_gradient(ctx.state0s[b], ctx.t0, ctx.t1, ctx.obs_times, g,
-                                            seg=ctx.seg, ckpts=ctx.ckpts[b])
-            return lam0[:, :, :W], adj
-
-        res = _per_experiment(one, B)
-        for s in ctx.streams:
-            main.wait_stream(s)
+        bp = ctx.bp
+        B, H, W, pitch = bp.B, bp.H, bp.W, bp.pitch
+        dev = bp.S.device
+        L = _lib()
+        seg, t1 = ctx.seg, ctx.t1
+        n_obs = len(ctx.obs_times)
+        g = torch.zeros((n_obs, B, 3, H, pitch), dtype=torch.float32, device=dev)
+        g[..., :W] = grad_out.to(torch.float32).transpose(0, 1)
+        obs_index = {}
+        for k, tt in enumerate(ctx.obs_times):
+            obs_index.setdefault(int(tt), []).append(k)
+        lam = torch.zeros((B, 3, H, pitch), dtype=torch.float32, device=dev)
+        lam_tmp = torch.empty_like(lam)
+        for k in obs_index.get(t1, []):
+            lam += g[k]
+        ns = 3 * H * pitch
+        buf = torch.empty((B, seg, 3, H, pitch), dtype=torch.float32, device=dev)
+        slots = int(L.fk_adjoint_slots(bp.grid))
+        gD = torch.zeros((B, H, pitch), dtype=torch.float32, device=dev)
+        gth = torch.zeros((B, slots, 16), dtype=torch.float64, device=dev)
+        wsb = int(L.fk_adjoint_batch_workspace_bytes(B))
+        ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+        stim_ptrs = (ctypes.POINTER(N.Stimulus) * B)(
+            *[ctypes.cast(a, ctypes.POINTER(N.Stimulus)) for a, _ in bp.stims])
+        n_stims = (ctypes.c_int * B)(*[n for _, n in bp.stims])
+        for s, st in reversed(ctx.ckpts):
+            e = min(s + seg, t1)
+            bp.S.copy_(st)
+            rc = L.fk_batch_recompute(bp.plan, s, e - s, buf.data_ptr(), seg * ns,
+                                      stream_handle())
+            if rc:
+                raise N.FkError(rc, "fk_batch_recompute")
+            inj = [(tt, k) for tt in range(s, e) for k in obs_index.get(tt, [])]
+            steps = (ctypes.c_int64 * max(1, len(inj)))(*[tt for tt, _ in inj])
+            grads = (ctypes.c_void_p * max(1, len(inj)))(*[g[k].data_ptr() for _, k in inj])
+            rc = L.fk_adjoint_batch_range(B, bp.grid, buf.data_ptr(), seg * ns, s, e - s,
+                                          bp.D.data_ptr(), ctypes.byref(bp.params), stim_ptrs,
+                                          n_stims, bp.dt, bp.dx, lam.data_ptr(),
+                                          lam_tmp.data_ptr(), steps, grads, len(inj),
+                                          gD.data_ptr(), gth.data_ptr(), ws.data_ptr(), wsb,
+                                          stream_handle())
+            if rc:
+                raise N.FkError(rc, "fk_adjoint_batch_range")
         ctx.ckpts = None
-        g0 = [r[0] for r in res]
-        adjs = [r[1] for r in res]
-        gD = adjs[0].grad_D().clone()
-        gth = adjs[0].grad_theta()
-        for a in adjs[1:]:  # fixed order: deterministic sums
-            gD += a.grad_D()
-            gth = gth + a.grad_theta()
-        return (torch.stack(g0), gD, gth.to(torch.float32), None, None, None, None, None, None,
-                None, None)
+        gD_sum = gD[0, :, :W].clone()
+        gth_sum = gth[0, :, :N_THETA].sum(0)
+        for b in range(1, B):  # fixed order: deterministic sums
+            gD_sum += gD[b, :, :W]
+            gth_sum = gth_sum + gth[b, :, :N_THETA].sum(0)
+        ctx.bp = None
+        bp.close()
+        return (lam[..., :W], gD_sum, gth_sum.to(torch.float32), None, None, None, None, None,
+                None, None, None)
 
 
 def rollout_batch(states0, D, theta, stimuli_per_tissue, t0: int, t1: int,

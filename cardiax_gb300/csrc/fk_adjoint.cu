@@ -324,7 +324,9 @@ constexpr int AYW = ATX + 4;  // row width of the y-derivative planes (tile colu
 // Interior cells (at least ADJ_BAND from both ends of an axis) use G^T = -G on central rows:
 // along x, A_x^T(D mu) = G G (D mu) / dx^2, B_x^T(D_x mu) = -G (D_x mu) / dx and
 // B_x^T(mu u_x) = -G (mu u_x) / dx, from first derivatives staged in shared memory.
-__global__ void __launch_bounds__(ANT) fk_adjoint_kernel(const __grid_constant__ AdjointArgs a) {
+// Tile (bx, by) of the step described by `a` (a kernel parameter, or a block's shared copy);
+// its dL/dtheta partial sums go to slot by * nbx + bx of a.gtheta.
+__device__ __forceinline__ void adjoint_tile(const AdjointArgs &a, int bx, int by, int nbx) {
     __shared__ float su[ASH * ASW], sd[ASH * ASW], sm[ASH * ASW];  // u, D, mu = dt lam'_u
     __shared__ float sux[(ATY + 4) * AXW], sqx[(ATY + 4) * AXW], sbx[(ATY + 4) * AXW];
     __shared__ float suy[ATY * AYW], sqy[ATY * AYW], sby[ATY * AYW];
@@ -332,7 +334,7 @@ __global__ void __launch_bounds__(ANT) fk_adjoint_kernel(const __grid_constant__
     const int tid = threadIdx.x;
     const int H = a.H, W = a.W, pitch = a.pitch;
     const float dt = a.dt, rdx = a.rdx;
-    const int i0 = blockIdx.y * ATY, j0 = blockIdx.x * ATX;
+    const int i0 = by * ATY, j0 = bx * ATX;
 
     // u, D, mu with a 4-cell halo; out-of-grid positions hold clamped copies, read only by
     // cells that take the explicit path along that axis
@@ -423,9 +425,44 @@ __global__ void __launch_bounds__(ANT) fk_adjoint_kernel(const __grid_constant__
         if (tid < kAdjParams) {
             double s = 0.0;
             for (int w = 0; w < ANT / 32; ++w) s += (double)red[tid][w];
-            a.gtheta[(int64_t)(blockIdx.y * gridDim.x + blockIdx.x) * kAdjParamStride + tid] += s;
+            a.gtheta[(int64_t)(by * nbx + bx) * kAdjParamStride + tid] += s;
         }
     }
+}
+
+__global__ void __launch_bounds__(ANT, 4) fk_adjoint_kernel(const __grid_constant__ AdjointArgs a) {
+    adjoint_tile(a, blockIdx.x, blockIdx.y, gridDim.x);
+}
+
+// One reverse step of many experiments (blockIdx.z): exps[e] describes step 0 of experiment e's
+// segment with the cotangent ping-pong buffers (lu.. = buffer A, olu.. = buffer B); step k reads
+// the state k * k_stride further on, and parity 1 swaps the two cotangent buffers.
+__global__ void __launch_bounds__(ANT, 4) fk_adjoint_batch_kernel(const AdjointArgs *__restrict__ exps,
+                                                               int64_t k_stride, int k, int parity,
+                                                               float t) {
+    __shared__ __align__(16) AdjointArgs sa;
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(exps + blockIdx.z);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(&sa);
+    for (int w = threadIdx.x; w < (int)(sizeof(AdjointArgs) / 4); w += ANT) dst[w] = __ldg(src + w);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int64_t o = (int64_t)k * k_stride;
+        sa.u += o;
+        sa.v += o;
+        sa.w += o;
+        sa.t = t;
+        if (parity) {
+            const float *lu = sa.lu, *lv = sa.lv, *lw = sa.lw;
+            sa.lu = sa.olu;
+            sa.lv = sa.olv;
+            sa.lw = sa.olw;
+            sa.olu = const_cast<float *>(lu);
+            sa.olv = const_cast<float *>(lv);
+            sa.olw = const_cast<float *>(lw);
+        }
+    }
+    __syncthreads();
+    adjoint_tile(sa, blockIdx.x, blockIdx.y, gridDim.x);
 }
 
 }  // namespace
@@ -437,6 +474,14 @@ int64_t adjoint_slots(int H, int W) {
 cudaError_t launch_adjoint(const AdjointArgs &a, cudaStream_t stream) {
     dim3 grid((a.W + ATX - 1) / ATX, (a.H + ATY - 1) / ATY);
     fk_adjoint_kernel<<<grid, ANT, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_batch(const AdjointArgs *exps, int n_exp, int H, int W, int64_t k_stride,
+                                 int k, int parity, float t, cudaStream_t stream) {
+    if (n_exp < 1) return cudaSuccess;
+    dim3 grid((W + ATX - 1) / ATX, (H + ATY - 1) / ATY, n_exp);
+    fk_adjoint_batch_kernel<<<grid, ANT, 0, stream>>>(exps, k_stride, k, parity, t);
     return cudaGetLastError();
 }
 

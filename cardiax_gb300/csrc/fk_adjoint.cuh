@@ -28,5 +28,9 @@ struct AdjointArgs {
 // Number of dL/dtheta slots (kAdjParamStride doubles each) written by launch_adjoint.
 int64_t adjoint_slots(int H, int W);
 cudaError_t launch_adjoint(const AdjointArgs &a, cudaStream_t stream);
+// Reverse step k of a segment for n_exp experiments of the same H x W grid (device descriptors
+// `exps`, see fk_adjoint_batch_kernel); parity selects the cotangent buffer read.
+cudaError_t launch_adjoint_batch(const AdjointArgs *exps, int n_exp, int H, int W, int64_t k_stride,
+                                 int k, int parity, float t, cudaStream_t stream);
 
 }  // namespace fk

@@ -289,6 +289,49 @@ int fk_batch_forward_euler(fk_batch *b, int64_t t0, int64_t t1, int graph_steps,
     return FK_OK;
 }
 
+// Copies the state held by buffer `parity` of every tissue (0: state, 1: scratch; three
+// consecutive planes) to dst + e * exp_stride (tissue e, all on one grid of `ns` floats).
+__global__ static void batch_state_out_kernel(const BatchTissue *tissues, int parity, float *dst,
+                                              int64_t exp_stride, int64_t ns) {
+    const float4 *src = reinterpret_cast<const float4 *>(tissues[blockIdx.y].args[parity].v);
+    float4 *out = reinterpret_cast<float4 *>(dst + (int64_t)blockIdx.y * exp_stride);
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ns / 4;
+         k += (int64_t)gridDim.x * blockDim.x)
+        out[k] = __ldcg(src + k);
+}
+
+int fk_batch_recompute(fk_batch *b, int64_t s, int64_t n, float *bufs, int64_t exp_stride,
+                       void *stream) {
+    if (!b || !bufs) return FK_ERR_NULL;
+    if (n < 1 || s < -(int64_t(1) << 24) || s + n > (int64_t(1) << 24)) return FK_ERR_ARGUMENT;
+    if (b->act) return FK_ERR_ARGUMENT;  // recomputed steps must not record activations again
+    const StepArgs &a0 = b->h_tissues[0].args[0];
+    for (int e = 1; e < b->n; ++e) {
+        const StepArgs &a = b->h_tissues[e].args[0];
+        if (a.H != a0.H || a.W != a0.W || a.pitch != a0.pitch) return FK_ERR_SHAPE;
+    }
+    const int64_t ns = 3 * (int64_t)a0.H * a0.pitch;
+    if (exp_stride < n * ns || (reinterpret_cast<uintptr_t>(bufs) & 15u) || (exp_stride & 3))
+        return FK_ERR_ALIGN;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev != b->device) return FK_ERR_CUDA;
+    cudaStream_t cs = (cudaStream_t)stream;
+    set_int_kernel<<<1, 1, 0, cs>>>(b->d_t, (int)s);
+    const dim3 cgrid(64, b->n);
+    batch_state_out_kernel<<<cgrid, 256, 0, cs>>>(b->d_tissues, 0, bufs, exp_stride, ns);
+    if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;
+    for (int64_t k = 1; k < n; ++k) {
+        // step s+k-1 reads buffer (k-1)&1 and leaves x_{s+k} in buffer k&1
+        if (launch_batch_step(b->d_tissues, b->d_maps, b->d_items, b->n_items, b->d_t, (int)(k - 1),
+                              (int)((k - 1) & 1), false, b->status, b->grid, cs) != cudaSuccess)
+            return FK_ERR_CUDA;
+        batch_state_out_kernel<<<cgrid, 256, 0, cs>>>(b->d_tissues, (int)(k & 1), bufs + k * ns,
+                                                      exp_stride, ns);
+        if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;
+    }
+    return FK_OK;
+}
+
 int fk_batch_destroy(fk_batch *b) {
     if (!b) return FK_ERR_NULL;
     release_graph(b);

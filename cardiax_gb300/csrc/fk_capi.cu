@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "../../include/cardiax_gb300.h"
 #include "fk_capi_internal.h"
@@ -765,6 +766,83 @@ int fk_adjoint_step(fk_grid g, const float *state, const float *D, const fk_para
     a.n_stim = n_stimuli;
     a.m = make_model(*p);
     return launch_adjoint(a, (cudaStream_t)stream) == cudaSuccess ? FK_OK : FK_ERR_CUDA;
+}
+
+size_t fk_adjoint_batch_workspace_bytes(int n_exp) {
+    if (n_exp <= 0) return 0;
+    return ((size_t)n_exp * sizeof(AdjointArgs) + 255) / 256 * 256;
+}
+
+int fk_adjoint_batch_range(int n_exp, fk_grid g, const float *bufs, int64_t exp_stride, int64_t s,
+                           int64_t n, const float *D, const fk_params *p,
+                           const fk_stimulus *const *stimuli, const int *n_stimuli, double dt,
+                           double dx, float *lam, float *lam_tmp, const int64_t *inj_steps,
+                           const float *const *inj_grads, int n_inj, float *grad_D,
+                           double *grad_theta_slots, void *workspace, size_t workspace_bytes,
+                           void *stream) {
+    int rc = common_checks(g, bufs, lam, D, p, dx);
+    if (rc) return rc;
+    if (!lam_tmp || !workspace || !stimuli || !n_stimuli ||
+        (n_inj > 0 && (!inj_steps || !inj_grads)))
+        return FK_ERR_NULL;
+    if (n_exp < 1 || n_exp > 65535 || n < 1 || n_inj < 0 || !std::isfinite(dt))
+        return FK_ERR_ARGUMENT;
+    const int64_t plane = g.H * g.pitch, ns = 3 * plane;
+    if (exp_stride < n * ns || (exp_stride & 3) || !aligned16(lam_tmp) || !aligned16(workspace) ||
+        (grad_D && !aligned16(grad_D)))
+        return FK_ERR_ALIGN;
+    if (workspace_bytes < fk_adjoint_batch_workspace_bytes(n_exp)) return FK_ERR_ARGUMENT;
+    const int64_t slots = adjoint_slots((int)g.H, (int)g.W);
+    std::vector<AdjointArgs> h((size_t)n_exp);
+    const Model m = make_model(*p);
+    for (int e = 0; e < n_exp; ++e) {
+        AdjointArgs &a = h[e];
+        a = AdjointArgs{};
+        if ((rc = make_stims(stimuli[e], n_stimuli[e], g, a.stim))) return rc;
+        const float *x = bufs + e * exp_stride;
+        float *la = lam + e * ns, *lb = lam_tmp + e * ns;
+        a.v = x;
+        a.w = x + plane;
+        a.u = x + 2 * plane;
+        a.D = D;
+        a.lv = la;
+        a.lw = la + plane;
+        a.lu = la + 2 * plane;
+        a.olv = lb;
+        a.olw = lb + plane;
+        a.olu = lb + 2 * plane;
+        a.gD = grad_D ? grad_D + e * plane : nullptr;
+        a.gtheta = grad_theta_slots ? grad_theta_slots + e * slots * kAdjParamStride : nullptr;
+        a.H = (int)g.H;
+        a.W = (int)g.W;
+        a.pitch = (int)g.pitch;
+        a.dt = (float)dt;
+        a.rdx = 1.0f / (float)dx;
+        a.n_stim = n_stimuli[e];
+        a.m = m;
+    }
+    cudaStream_t cs = (cudaStream_t)stream;
+    AdjointArgs *dexp = static_cast<AdjointArgs *>(workspace);
+    if (cudaMemcpyAsync(dexp, h.data(), sizeof(AdjointArgs) * h.size(), cudaMemcpyHostToDevice,
+                        cs) != cudaSuccess)
+        return FK_ERR_CUDA;
+    // reverse step r (k = n-1-r) reads buffer r&1 (0: lam, 1: lam_tmp) and writes the other
+    for (int64_t k = n - 1, r = 0; k >= 0; --k, ++r) {
+        if (launch_adjoint_batch(dexp, n_exp, (int)g.H, (int)g.W, ns, (int)k, (int)(r & 1),
+                                 (float)(s + k), cs) != cudaSuccess)
+            return FK_ERR_CUDA;
+        float *cur = (r & 1) ? lam : lam_tmp;
+        for (int j = 0; j < n_inj; ++j)
+            if (inj_steps[j] == s + k) {
+                add_state_kernel<<<1024, 256, 0, cs>>>(cur, inj_grads[j], n_exp * ns);
+                if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;
+            }
+    }
+    if (((n - 1) & 1) == 0 &&  // the last step wrote lam_tmp
+        cudaMemcpyAsync(lam, lam_tmp, sizeof(float) * n_exp * ns, cudaMemcpyDeviceToDevice, cs) !=
+            cudaSuccess)
+        return FK_ERR_CUDA;
+    return FK_OK;
 }
 
 int fk_recompute(fk_grid g, const float *state, int64_t s, int64_t n, const float *D,

@@ -266,6 +266,33 @@ int fk_adjoint_range(fk_grid g, const float *buf, int64_t s, int64_t n, const fl
                      const float *const *inj_grads, int n_inj, float *grad_D,
                      double *grad_theta_slots, void *stream);
 
+/* Batched reverse pass: E experiments on one grid that share D and the parameters (each with
+ * its own stimuli and state), as in an inverse problem fitted to several recordings.  No
+ * reference counterpart.  Per experiment the results equal fk_recompute / fk_adjoint_range bit
+ * for bit; every step is one launch for all experiments.
+ *
+ * fk_batch_recompute: `plan` holds the E experiments as its tissues (one grid, no activation
+ * tracking); each tissue's state buffer holds x_s on entry.  Writes x_s .. x_{s+n-1} of tissue
+ * e to bufs + e * exp_stride + k * 3 * H * pitch (k = 0 .. n-1); the tissues' state and scratch
+ * buffers are overwritten.
+ *
+ * fk_adjoint_batch_range: fk_adjoint_range for every experiment e, its segment states at
+ * bufs + e * exp_stride, its stimuli stimuli[e] (n_stimuli[e] entries).  lam and lam_tmp hold E
+ * consecutive states (experiment e at + e * 3 * H * pitch), inj_grads[j] E consecutive states,
+ * grad_D E consecutive planes and grad_theta_slots E * fk_adjoint_slots(g) slots.  `workspace`
+ * is device memory of fk_adjoint_batch_workspace_bytes(E) bytes (16-byte aligned) that receives
+ * the experiments' descriptors. */
+size_t fk_adjoint_batch_workspace_bytes(int n_exp);
+int fk_batch_recompute(fk_batch *plan, int64_t s, int64_t n, float *bufs, int64_t exp_stride,
+                       void *stream);
+int fk_adjoint_batch_range(int n_exp, fk_grid g, const float *bufs, int64_t exp_stride, int64_t s,
+                           int64_t n, const float *D, const fk_params *p,
+                           const fk_stimulus *const *stimuli, const int *n_stimuli, double dt,
+                           double dx, float *lam, float *lam_tmp, const int64_t *inj_steps,
+                           const float *const *inj_grads, int n_inj, float *grad_D,
+                           double *grad_theta_slots, void *workspace, size_t workspace_bytes,
+                           void *stream);
+
 #ifdef __cplusplus
 }
 #endif

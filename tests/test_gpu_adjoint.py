@@ -156,3 +156,46 @@ def test_batched_rollout_equals_single_rollouts():
     # to the largest entry, as cancellation leaves a few entries near zero
     torch.testing.assert_close(gD_b, D.grad, rtol=1e-5, atol=1e-5 * D.grad.abs().max().item())
     torch.testing.assert_close(gth_b, th.grad, rtol=1e-5, atol=1e-5 * th.grad.abs().max().item())
+
+
+@pytest.mark.parametrize("shape,seg,obs", [((40, 52), 7, [0, 10, 30]), ((33, 130), 5, [12, 23])])
+def test_batched_reverse_pass_equals_per_experiment_bit_for_bit(shape, seg, obs):
+    """rollout_batch runs the forward, the segment recomputation and the adjoint as one launch
+    per step for all experiments; per experiment that is the same arithmetic as the experiment's
+    own reverse pass (Adjoint.rollout_gradient on its Tissue), so the cotangent of the initial
+    state matches bit for bit, and dL/dD, dL/dtheta are the experiment-order sums of the
+    per-experiment values.  Several segments (seg 5, 7), observations on a segment boundary and at
+    the first step."""
+    _gpu()
+    from cardiax_gb300.adjoint import Adjoint, rollout_batch
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    from cardiax_gb300.tissue import Tissue
+    dev = torch.device("cuda", 0)
+    H, W = shape
+    cases = [_case(shape, s) for s in (31, 32, 33)]
+    Dn = cases[0][3].astype(np.float32)
+    D = torch.tensor(Dn, device=dev, requires_grad=True)
+    th = torch.tensor(P3[:13], dtype=torch.float32, device=dev, requires_grad=True)
+    s0 = torch.tensor(np.stack([np.stack(c[:3]) for c in cases]), dtype=torch.float32, device=dev,
+                      requires_grad=True)
+    stims = [[Stimulus(Protocol(*c[4][:3]), c[4][3].astype(np.float32))] for c in cases]
+    rng = np.random.default_rng(5)
+    R = torch.tensor(rng.standard_normal((3, len(obs), 3, H, W)), dtype=torch.float32, device=dev)
+    out = rollout_batch(s0, D, th, stims, 0, max(obs), obs, seg=seg)
+    (out * R).sum().backward()
+
+    gD_sum, gth_sum = None, None
+    for b in range(3):
+        tis = Tissue(shape, list(P3), Dn, stims[b], device=dev)
+        tis.set_state(s0[b].detach())
+        state0 = tis.state.clone()
+        adj = Adjoint(tis)
+        g = torch.zeros((len(obs),) + tuple(state0.shape), dtype=torch.float32, device=dev)
+        g[..., :W] = R[b]
+        lam0 = adj.rollout_gradient(state0, 0, max(obs), obs, g, seg=seg)
+        torch.cuda.synchronize()
+        assert torch.equal(lam0[..., :W], s0.grad[b]), b
+        gD_sum = adj.grad_D().clone() if gD_sum is None else gD_sum + adj.grad_D()
+        gth_sum = adj.grad_theta() if gth_sum is None else gth_sum + adj.grad_theta()
+    assert torch.equal(gD_sum, D.grad)
+    assert torch.equal(gth_sum.to(torch.float32), th.grad)
