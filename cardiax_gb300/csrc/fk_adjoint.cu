@@ -314,6 +314,30 @@ __device__ AxisTerms axis_edge(const AdjointArgs &a, int i, int j) {
     return t;
 }
 
+// axis_edge from a line's precomputed products (L[r] = (D mu, (B D) mu, u, mu u_x) at the r-th
+// cell from the near end) and the corner tables in shared memory: the same fused multiply-adds
+// in the same order, so the same bits.
+__device__ __forceinline__ AxisTerms axis_edge_tab(const float4 *L, const float (*tA)[10],
+                                                   const float (*tB)[10], int pp, bool near0,
+                                                   float rdx) {
+    float AT = 0.f, BT = 0.f, d2 = 0.f, g = 0.f;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const float4 l = L[r];
+        AT = fmaf(tA[r][pp], l.x, AT);
+        BT = fmaf(tB[r][pp], l.y, BT);
+        d2 = fmaf(tA[pp][r], l.z, d2);
+        g = fmaf(tB[r][pp], l.w, g);
+    }
+    const float sgn = near0 ? 1.0f : -1.0f;
+    AxisTerms t;
+    t.AT = AT * (rdx * rdx);
+    t.BT = sgn * BT * rdx;
+    t.d2 = d2 * (rdx * rdx);
+    t.g = sgn * g * rdx;
+    return t;
+}
+
 // Tile geometry: ATY x ATX cells per block, a 4-cell halo of u, D and mu in shared memory.
 constexpr int ATX = 32, ATY = 16, AHALO = 4;
 constexpr int ASW = ATX + 2 * AHALO, ASH = ATY + 2 * AHALO;
@@ -331,10 +355,21 @@ __device__ __forceinline__ void adjoint_tile(const AdjointArgs &a, int bx, int b
     __shared__ float sux[(ATY + 4) * AXW], sqx[(ATY + 4) * AXW], sbx[(ATY + 4) * AXW];
     __shared__ float suy[ATY * AYW], sqy[ATY * AYW], sby[ATY * AYW];
     __shared__ float red[kAdjParams][ANT / 32];
+    // edge band: per line and end, the 10 products each band cell of that line needs (ex: the
+    // x-direction lines of the tile's columns, ey: the y-direction lines of its rows), and the
+    // corner tables (lanes of a column band index them with different pp)
+    __shared__ float4 ex[2][ATX][10], ey[2][ATY][10];
+    __shared__ float tA[10][10], tB[10][10];
     const int tid = threadIdx.x;
     const int H = a.H, W = a.W, pitch = a.pitch;
     const float dt = a.dt, rdx = a.rdx;
     const int i0 = by * ATY, j0 = bx * ATX;
+    // which line ends have the cells their products read -- -1 .. 11 from the near end, the pad
+    // cell included (a clamped copy in the halo) -- inside the shared halo (uniform per block)
+    const bool tx0 = H >= kEdgeMinLine && i0 == 0;
+    const bool tx1 = H >= kEdgeMinLine && i0 + ATY > H - ADJ_BAND && i0 <= H - 8 && i0 + ATY + 3 >= H;
+    const bool ty0 = W >= kEdgeMinLine && j0 == 0;
+    const bool ty1 = W >= kEdgeMinLine && j0 + ATX > W - ADJ_BAND && j0 <= W - 8 && j0 + ATX + 3 >= W;
 
     // u, D, mu with a 4-cell halo; out-of-grid positions hold clamped copies, read only by
     // cells that take the explicit path along that axis
@@ -347,6 +382,39 @@ __device__ __forceinline__ void adjoint_tile(const AdjointArgs &a, int bx, int b
         sm[k] = dt * __ldg(a.lu + g);
     }
     __syncthreads();
+    // edge-band line products from the shared halo (edge tiles only)
+    if (tx0 || tx1 || ty0 || ty1) {
+        for (int k = tid; k < 200; k += ANT) {
+            const int r = k / 10, c = k % 10;
+            if (r < 10) tA[r][c] = kEdge.A[r][c];
+            else tB[r - 10][c] = kEdge.B[r - 10][c];
+        }
+        const int nx = (tx0 + tx1) * ATX * 10, ny = (ty0 + ty1) * ATY * 10;
+        for (int k = tid; k < nx + ny; k += ANT) {
+            if (k < nx) {
+                const int e = (!tx0 || k >= ATX * 10) ? 1 : 0;
+                const int kk = k - (tx0 && e == 1 ? ATX * 10 : 0);
+                const int c = kk / 10, r = kk % 10;
+                const int q = e ? H - 1 - r : r;
+                auto SR = [&](const float *f, int x) { return f[(x - i0 + AHALO) * ASW + c + AHALO]; };
+                const float mu = SR(sm, q);
+                const float dq = fwd_d1([&](int x) { return SR(sd, x); }, q, H) * rdx;
+                const float uq = fwd_d1([&](int x) { return SR(su, x); }, q, H) * rdx;
+                ex[e][c][r] = make_float4(SR(sd, q) * mu, dq * mu, SR(su, q), mu * uq);
+            } else {
+                const int k2 = k - nx;
+                const int e = (!ty0 || k2 >= ATY * 10) ? 1 : 0;
+                const int kk = k2 - (ty0 && e == 1 ? ATY * 10 : 0);
+                const int rr = kk / 10, r = kk % 10;
+                const int q = e ? W - 1 - r : r;
+                auto SC = [&](const float *f, int y) { return f[(rr + AHALO) * ASW + y - j0 + AHALO]; };
+                const float mu = SC(sm, q);
+                const float dq = fwd_d1([&](int y) { return SC(sd, y); }, q, W) * rdx;
+                const float uq = fwd_d1([&](int y) { return SC(su, y); }, q, W) * rdx;
+                ey[e][rr][r] = make_float4(SC(sd, q) * mu, dq * mu, SC(su, q), mu * uq);
+            }
+        }
+    }
     // x: u_x, G_x(D mu), D_x mu on tile rows -2 .. ATY+1
     for (int k = tid; k < (ATY + 4) * AXW; k += ANT) {
         const int r = k / AXW, c = k % AXW;
@@ -391,7 +459,11 @@ __device__ __forceinline__ void adjoint_tile(const AdjointArgs &a, int bx, int b
             x.g = -g_central(M(-2) * X(sux, -2), M(-1) * X(sux, -1), M(1) * X(sux, 1),
                              M(2) * X(sux, 2)) * rdx;
         } else {
-            x = axis_edge<0>(a, i, j);
+            const bool near0 = i < ADJ_BAND;
+            if (near0 ? tx0 : tx1)
+                x = axis_edge_tab(ex[near0 ? 0 : 1][c], tA, tB, near0 ? i : H - 1 - i, near0, rdx);
+            else
+                x = axis_edge<0>(a, i, j);
         }
         if (j >= ADJ_BAND && j < W - ADJ_BAND) {
             auto Y = [&](const float *f, int d) { return f[r * AYW + c + 2 + d]; };
@@ -402,7 +474,11 @@ __device__ __forceinline__ void adjoint_tile(const AdjointArgs &a, int bx, int b
             y.g = -g_central(M(-2) * Y(suy, -2), M(-1) * Y(suy, -1), M(1) * Y(suy, 1),
                              M(2) * Y(suy, 2)) * rdx;
         } else {
-            y = axis_edge<1>(a, i, j);
+            const bool near0 = j < ADJ_BAND;
+            if (near0 ? ty0 : ty1)
+                y = axis_edge_tab(ey[near0 ? 0 : 1][r], tA, tB, near0 ? j : W - 1 - j, near0, rdx);
+            else
+                y = axis_edge<1>(a, i, j);
         }
         const float diff_u = (x.AT + y.AT) + (x.BT + y.BT);
         const float gD = mu * (x.d2 + y.d2) + (x.g + y.g);
