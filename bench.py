@@ -154,7 +154,8 @@ def run_adjoint(dev, n_tissues: int = 16, steps: int = 5000, n_obs: int = 20, si
     scar-D tissue (parameter set 3), each with its own 10x10 point stimulus; observations of u
     at 20 evenly spaced checkpoints over 5000 steps; MSE loss against observations made with the
     true D; gradient w.r.t. D (65,536 values, shared by the batch) and the 13 parameters through
-    the adjoint kernel with sqrt(T) checkpointing (one CUDA stream per experiment).
+    the adjoint kernel with sqrt(T) checkpointing (forward, segment recomputation and adjoint
+    each one launch per step for all 16 experiments).
     ``grad_steps_per_s`` = experiments x steps / seconds of forward + backward."""
     import torch
     from cardiax_gb300 import params as Pm
