@@ -344,6 +344,60 @@ def run_reference(args):
 METRIC = "GCUPS (1e9 Fenton-Karma cell-updates/s), fused FP32 Euler stepper; roofline.frac = % of HBM roofline"
 
 
+def run_next_rows(dev, reps: int = 2):
+    """The callers either side of the stepper, each timed on the device (best of ``reps``):
+
+    * ``heun``: the Heun integrator (cardiax/solve.py:73-85,103-111) on the 2048^2 roofline
+      workload, 2000 steps, GCUPS;
+    * ``sequence``: deepx/generate.py:135-210 as the reference's data generation runs it --
+      a 1200^2 tissue from rest, two triangular stimuli (modulus 20, 2 steps), 10 000 Euler
+      steps, the state emitted every 100 steps resized to 256^2 on the device -- GCUPS of the
+      stepping with the emission included, and emitted states per second."""
+    import torch
+    from cardiax_gb300 import generate, params as Pm
+    from cardiax_gb300.stimulus import Direction, Protocol, Stimulus, triangular
+    from cardiax_gb300.tissue import Tissue
+
+    def best(fn):
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+
+    H = W = 2048
+    D = noisy_diffusivity(H, W, seed=1)
+    f = np.zeros((H, W), np.float32)
+    f[:, :5] = 20.0
+    tis = Tissue((H, W), Pm.PARAMSET_3, D, [Stimulus(Protocol(0, 200, 20000), f)], device=dev)
+    n_heun = 2000
+
+    def heun():
+        tis.init()
+        tis.advance_heun(0, n_heun)
+    t_h = best(heun)
+    heun_r = {"size": f"{H}x{W}", "steps": n_heun, "gcups": H * W * n_heun / t_h / 1e9,
+              "us_per_step": t_h / n_heun * 1e6}
+
+    S, n_steps, every, out = 1200, 10000, 100, (256, 256)
+    Ds = np.full((S, S), 1e-3, np.float32)
+    stims = [triangular((S, S), Direction.WEST, 30.0, 0.2, 20.0, Protocol(0, 2, 1e9), device=dev),
+             triangular((S, S), Direction.SOUTH, -45.0, 0.2, 20.0, Protocol(3000, 2, 1e9),
+                        device=dev)]
+
+    def seq():
+        generate.sequence(0, n_steps + every, every, 0.01, 0.01, Pm.PARAMSET_3, Ds, stims,
+                          reshape=out, device=dev)
+    t_s = best(seq)
+    seq_r = {"grid": f"{S}x{S}", "euler_steps": n_steps, "emit_every": every,
+             "reshape": f"{out[0]}x{out[1]}", "gcups": S * S * n_steps / t_s / 1e9,
+             "states_per_s": (n_steps // every) / t_s}
+    return {"heun": heun_r, "sequence": seq_r}
+
+
 def run_schedules(dev, sizes=(1024, 2048), steps: int = 400):
     """GCUPS of each stepping schedule on the roofline workload (best of 2 runs of ``steps``
     steps, L2 flushed before each run)."""
@@ -493,6 +547,9 @@ def run_ours(args):
     schedules = None
     if not args.no_schedules:
         schedules = run_schedules(dev)
+    next_rows = None
+    if not args.no_next:
+        next_rows = run_next_rows(dev)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -509,7 +566,7 @@ def run_ours(args):
                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
                "config": config(args), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                "gpu_launches": args.steps * (S + 1), "clocks": clk, "batched": batched,
-               "adjoint": adjoint, "schedules": schedules,
+               "adjoint": adjoint, "schedules": schedules, "next_rows": next_rows,
                "wall_s_timed_region": t_wall}
         print(json.dumps(out))
     if world > 1:
@@ -532,6 +589,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-schedules", action="store_true")
+    ap.add_argument("--no-next", action="store_true", help="skip the Heun and sequence timings")
     ap.add_argument("--batched-steps", type=int, default=2000)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -199,10 +199,12 @@ struct MapCache {
 static int g_step_kernel = 0;
 
 // One step from `in` to `out` (Euler, or the derivative with `deriv`).
+// heun: 0 = an Euler step (or the derivative); 1, 2 = the Heun stages (StepArgs: dso, x0, d1, h).
 int step_once(const fk_grid &g, const float *in, float *out, const float *D, const Model &m,
               const Stim *st, int ns, int64_t t, float dt, float rdx, bool deriv,
               const CUtensorMap &tm_d, MapCache &maps, int *status, cudaStream_t stream,
-              const fk_activation *act = nullptr) {
+              const fk_activation *act = nullptr, int heun = 0, float *dso = nullptr,
+              const float *x0 = nullptr, const float *d1 = nullptr, float h = 0.0f) {
     const int64_t plane = g.H * g.pitch;
     StepMaps sm;
     int rc = maps.get(g, in, out, sm);
@@ -233,8 +235,14 @@ int step_once(const fk_grid &g, const float *in, float *out, const float *D, con
         a.act_count = act->count;
         a.act_threshold = act->threshold;
     }
+    a.dso = dso;
+    a.x0 = x0;
+    a.d1 = d1;
+    a.h = h;
     cudaError_t e;
-    if (!deriv && g_step_kernel == 1 && strip_eligible(g.H, g.W)) {
+    if (heun) {
+        e = launch_step(sm, a, false, stream, heun);
+    } else if (!deriv && g_step_kernel == 1 && strip_eligible(g.H, g.W)) {
         StripMaps xm;
         if ((rc = maps.get_strip(g, in, D, xm))) return rc;
         e = launch_strip(xm, a, stream);
@@ -338,20 +346,6 @@ __global__ void add_state_kernel(float *dst, const float *src, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x)
         dst[i] += src[i];
-}
-
-// x1 = x + dt d (the first Heun stage; the same fused multiply-add as the Euler kernels)
-__global__ void heun_stage1_kernel(float *x1, const float *x, const float *d, float dt, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x)
-        x1[i] = fmaf(d[i], dt, x[i]);
-}
-// out = x + (d1 + d2) h, h = dt / 2 (cardiax/solve.py:80-84)
-__global__ void heun_combine_kernel(float *out, const float *x, const float *d1, const float *d2,
-                                    float h, int64_t n) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x)
-        out[i] = fmaf(d1[i] + d2[i], h, x[i]);
 }
 
 __global__ void fill_state_kernel(float *s, int64_t plane) {
@@ -618,20 +612,20 @@ int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, co
                                     nullptr, stream);
 }
 
-// One Heun step from `in` to `out` with work = [d1, x1, d2].
+// One Heun step from `in` to `out` with work = [d1, x1, ...]: two launches of the step kernel.
+// Stage 1 is the Euler step x1 = x + dt d1 that also stores d1 = f(x, t); stage 2 evaluates
+// f(x1, t) and writes x + (d1 + f(x1, t)) dt/2 -- per cell the operations of the derivative,
+// x1 = fmaf(d1, dt, x) and fmaf(d1 + d2, dt/2, x) of cardiax/solve.py:73-85.
 static int heun_once(const fk_grid &g, const float *in, float *out, float *work, const float *D,
                      const Model &m, const Stim *st, int ns, int64_t t, float dt, float rdx,
                      const CUtensorMap &tm_d, MapCache &maps, int *status, cudaStream_t s) {
     const int64_t n = 3 * g.H * g.pitch;
-    float *d1 = work, *x1 = work + n, *d2 = work + 2 * n;
-    int rc = step_once(g, in, d1, D, m, st, ns, t, 0.0f, rdx, true, tm_d, maps, status, s);
+    float *d1 = work, *x1 = work + n;
+    int rc = step_once(g, in, x1, D, m, st, ns, t, dt, rdx, false, tm_d, maps, status, s, nullptr,
+                       1, d1);
     if (rc) return rc;
-    heun_stage1_kernel<<<1024, 256, 0, s>>>(x1, in, d1, dt, n);
-    if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;
-    if ((rc = step_once(g, x1, d2, D, m, st, ns, t, 0.0f, rdx, true, tm_d, maps, status, s)))
-        return rc;
-    heun_combine_kernel<<<1024, 256, 0, s>>>(out, in, d1, d2, dt * 0.5f, n);
-    return cudaGetLastError() == cudaSuccess ? FK_OK : FK_ERR_CUDA;
+    return step_once(g, x1, out, D, m, st, ns, t, dt, rdx, false, tm_d, maps, status, s, nullptr, 2,
+                     nullptr, in, d1, dt * 0.5f);
 }
 
 int fk_heun_step(fk_grid g, const float *state, const float *D, const fk_params *p,

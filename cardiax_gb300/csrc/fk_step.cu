@@ -58,7 +58,7 @@ struct TileOrder {
 };
 
 // ---- the step kernel: persistent CTAs over the tiles of one tissue ------------------------
-template <bool DERIV, bool ACT>
+template <bool DERIV, bool ACT, int HEUN>
 __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_constant__ StepMaps tm,
                                                         const __grid_constant__ StepArgs a,
                                                         const __grid_constant__ PackConsts k) {
@@ -137,8 +137,9 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
             if (tid == 0 && ahead < ntiles) issue(ahead, (n + NSTAGE - 1) % NSTAGE);
         };
         float *ux_n = sux + (n & 1) * (TX * SUX_H), *uy_n = suy + (n & 1) * (SW * TY);
-        if (!process_tile<DERIV, ACT, true, true>(*sa, a.t, stage_at(smem, s), ux_n, uy_n, io,
-                                                  active, i0, j0, NoHook{}, &k, ok, refill)) {
+        if (!process_tile<DERIV, ACT, true, true, HEUN>(*sa, a.t, stage_at(smem, s), ux_n, uy_n,
+                                                        io, active, i0, j0, NoHook{}, &k, ok,
+                                                        refill)) {
             if (tid == 0) atomicOr(a.status, kStatusTimeout);
             return;
         }
@@ -270,9 +271,9 @@ cudaError_t launch_batch_copyback(const BatchTissue *tissues, int n_tissues, cud
     return cudaGetLastError();
 }
 
-template <bool DERIV, bool ACT>
+template <bool DERIV, bool ACT, int HEUN = 0>
 static cudaError_t set_smem_attr() {
-    return cudaFuncSetAttribute(fk_step_kernel<DERIV, ACT>,
+    return cudaFuncSetAttribute(fk_step_kernel<DERIV, ACT, HEUN>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_STEP_DIRECT_BYTES);
 }
 
@@ -292,7 +293,8 @@ bool l2_fits_step(int64_t H, int64_t pitch) {
     return 4 * H * pitch * (int64_t)sizeof(float) * 4 <= 3 * l2_bytes;
 }
 
-cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream) {
+cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream,
+                        int heun) {
     // the attribute is per function and per device; setting it is cheap and idempotent
     static thread_local int configured_device = -1;
     int dev = -1;
@@ -302,6 +304,8 @@ cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cud
         if ((e = set_smem_attr<true, false>()) != cudaSuccess) return e;
         if ((e = set_smem_attr<false, true>()) != cudaSuccess) return e;
         if ((e = set_smem_attr<false, false>()) != cudaSuccess) return e;
+        if ((e = set_smem_attr<false, false, 1>()) != cudaSuccess) return e;
+        if ((e = set_smem_attr<false, false, 2>()) != cudaSuccess) return e;
         configured_device = dev;
     }
     static thread_local int n_sm = 0;
@@ -320,9 +324,11 @@ cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cud
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const PackConsts k = make_pack_consts(a.m, a.rdx, a.dt);
-    if (deriv) return cudaLaunchKernelEx(&cfg, fk_step_kernel<true, false>, maps, a, k);
-    if (a.act_last) return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, true>, maps, a, k);
-    return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, false>, maps, a, k);
+    if (deriv) return cudaLaunchKernelEx(&cfg, fk_step_kernel<true, false, 0>, maps, a, k);
+    if (heun == 1) return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, false, 1>, maps, a, k);
+    if (heun == 2) return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, false, 2>, maps, a, k);
+    if (a.act_last) return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, true, 0>, maps, a, k);
+    return cudaLaunchKernelEx(&cfg, fk_step_kernel<false, false, 0>, maps, a, k);
 }
 
 }  // namespace fk

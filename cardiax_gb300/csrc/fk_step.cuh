@@ -75,6 +75,12 @@ struct StepArgs {
     // nonzero: the step's live data (the new state and D) fits in L2, so the step kernel marks
     // the input state's reads evict-first and D's evict-last (set by the host per device)
     int l2_hints;
+    // Heun stages (cardiax/solve.py:73-85; fk_step_kernel only).  Stage 1 is the Euler step
+    // x1 = x + dt d1 that also stores d1 = f(x, t) to `dso`; stage 2 reads x1 (the input state),
+    // x0 = x and d1, and writes x0 + (d1 + f(x1, t)) h with h = dt / 2.  Three planes each.
+    float *dso;
+    const float *x0, *d1;
+    float h;
 };
 
 enum : int { kStatusTimeout = 1 };
@@ -89,7 +95,8 @@ struct StepMaps {
 // Euler step also records activations: a cell whose u goes from below the threshold to at or
 // above it during step t -> t+1 gets act_last = t+1, act_first = t+1 if it was -1, and
 // act_count + 1.
-cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream);
+cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream,
+                        int heun = 0);
 // Whether one step's live data on an H x pitch grid fits in L2 (sets StepArgs::l2_hints).
 bool l2_fits_step(int64_t H, int64_t pitch);
 

@@ -74,7 +74,7 @@ struct OutTile {
 
 template <bool ACT>
 __device__ __noinline__ void boundary_cell(const StepArgs &a, float t, unsigned active, bool deriv,
-                                           int i, int j, const OutTile &o) {
+                                           int i, int j, const OutTile &o, int heun = 0) {
     const Clamped U{a.u, a.H, a.W, a.pitch}, D{a.D, a.H, a.W, a.pitch};
     const int H = a.H, W = a.W;
     const float rdx = a.rdx;
@@ -115,15 +115,25 @@ __device__ __noinline__ void boundary_cell(const StepArgs &a, float t, unsigned 
     }
     const float du = diffusion(d, dxD, dyD, UX(i), UY(j), uxx, uyy) + r.j_ion;
     float ov, ow, ou;
+    const int64_t plane = (int64_t)a.H * a.pitch;
     if (deriv) {
         ov = r.dv;
         ow = r.dw;
         ou = du;
+    } else if (heun == 2) {  // x0 + (d1 + d2) h, d2 = this cell's derivative at x1
+        ov = fmaf(__ldcg(a.d1 + off) + r.dv, a.h, __ldcg(a.x0 + off));
+        ow = fmaf(__ldcg(a.d1 + plane + off) + r.dw, a.h, __ldcg(a.x0 + plane + off));
+        ou = fmaf(__ldcg(a.d1 + 2 * plane + off) + du, a.h, __ldcg(a.x0 + 2 * plane + off));
     } else {
         ov = fmaf(r.dv, a.dt, v);
         ow = fmaf(r.dw, a.dt, w);
         ou = fmaf(du, a.dt, u);
         if (ACT) record_activation(a, t, off, u, ou);
+        if (heun == 1) {
+            __stcg(a.dso + off, r.dv);
+            __stcg(a.dso + plane + off, r.dw);
+            __stcg(a.dso + 2 * plane + off, du);
+        }
     }
     if (o.v) {
         const int lo = (i - o.i0) * TX + (j - o.j0);
@@ -165,7 +175,7 @@ static __device__ __noinline__ float4 apply_stimuli(const StepArgs &a, unsigned 
 // takes ceil(count / NT) of them: a top strip, a bottom strip, and left/right strips between.
 template <bool ACT>
 __device__ __noinline__ void boundary_band(const StepArgs &a, float t, unsigned active, bool deriv,
-                                           int i0, int j0, const OutTile &o) {
+                                           int i0, int j0, const OutTile &o, int heun = 0) {
     const int H = a.H, W = a.W;
     const int i1 = min(i0 + TY, H), j1 = min(j0 + TX, W);
     const int jw = j1 - j0;
@@ -190,7 +200,7 @@ __device__ __noinline__ void boundary_band(const StepArgs &a, float t, unsigned 
             i = ri0 + r;
             j = c < wl ? j0 + c : rj1 + (c - wl);
         }
-        boundary_cell<ACT>(a, t, active, deriv, i, j, o);
+        boundary_cell<ACT>(a, t, active, deriv, i, j, o, heun);
     }
 }
 
@@ -319,7 +329,8 @@ static __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_ro
 struct NoHook {
     __device__ void operator()() const {}
 };
-template <bool DERIV, bool ACT, bool EDGE, bool PK, bool DIRECT = false, class P1, class P2 = NoHook>
+template <bool DERIV, bool ACT, bool EDGE, bool PK, bool DIRECT = false, int HEUN = 0, class P1,
+          class P2 = NoHook>
 __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts *pk, float t,
                                              const Stage &st, float *sux, float *suy,
                                              const TileIO &io, unsigned active, int i0, int j0,
@@ -542,6 +553,25 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                 nw_hi = rh.dw;
                 nu_lo = du_lo;
                 nu_hi = du_hi;
+            } else if (HEUN == 2) {  // x0 + (d1 + d2) h; the input state is x1
+                const int64_t pl = (int64_t)H * pitch;
+                const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+                float4 xv = z, xw = z, xu = z, dv1 = z, dw1 = z, du1 = z;
+                if (i < H && j < W) {
+                    xv = __ldcg(reinterpret_cast<const float4 *>(a.x0 + goff));
+                    xw = __ldcg(reinterpret_cast<const float4 *>(a.x0 + pl + goff));
+                    xu = __ldcg(reinterpret_cast<const float4 *>(a.x0 + 2 * pl + goff));
+                    dv1 = __ldcg(reinterpret_cast<const float4 *>(a.d1 + goff));
+                    dw1 = __ldcg(reinterpret_cast<const float4 *>(a.d1 + pl + goff));
+                    du1 = __ldcg(reinterpret_cast<const float4 *>(a.d1 + 2 * pl + goff));
+                }
+                const float2 hh = mk2(a.h, a.h);
+                nv_lo = p_fma(p_add(mk2(dv1.x, dv1.y), rl.dv), hh, mk2(xv.x, xv.y));
+                nv_hi = p_fma(p_add(mk2(dv1.z, dv1.w), rh.dv), hh, mk2(xv.z, xv.w));
+                nw_lo = p_fma(p_add(mk2(dw1.x, dw1.y), rl.dw), hh, mk2(xw.x, xw.y));
+                nw_hi = p_fma(p_add(mk2(dw1.z, dw1.w), rh.dw), hh, mk2(xw.z, xw.w));
+                nu_lo = p_fma(p_add(mk2(du1.x, du1.y), du_lo), hh, mk2(xu.x, xu.y));
+                nu_hi = p_fma(p_add(mk2(du1.z, du1.w), du_hi), hh, mk2(xu.z, xu.w));
             } else {
                 nv_lo = p_fma(rl.dv, kc.dt, v_lo);
                 nv_hi = p_fma(rh.dv, kc.dt, v_hi);
@@ -560,20 +590,38 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
             };
             if constexpr (DIRECT) {
                 if (i < H && j < W) {
+                    const int64_t pl = (int64_t)H * pitch;
+                    // Heun stage 1 also stores d1 (the derivative at the input state)
+                    const float4 d4v = make_float4(rl.dv.x, rl.dv.y, rh.dv.x, rh.dv.y);
+                    const float4 d4w = make_float4(rl.dw.x, rl.dw.y, rh.dw.x, rh.dw.y);
+                    const float4 d4u = make_float4(du_lo.x, du_lo.y, du_hi.x, du_hi.y);
                     if (!band_mask && j + 3 < W) {
                         __stcg(reinterpret_cast<float4 *>(a.vo + goff), ov4);
                         __stcg(reinterpret_cast<float4 *>(a.wo + goff), ow4);
                         __stcg(reinterpret_cast<float4 *>(a.uo + goff), ou4);
+                        if (HEUN == 1) {
+                            __stcg(reinterpret_cast<float4 *>(a.dso + goff), d4v);
+                            __stcg(reinterpret_cast<float4 *>(a.dso + pl + goff), d4w);
+                            __stcg(reinterpret_cast<float4 *>(a.dso + 2 * pl + goff), d4u);
+                        }
                     } else {
                         const float fv[4] = {ov4.x, ov4.y, ov4.z, ov4.w};
                         const float fw[4] = {ow4.x, ow4.y, ow4.z, ow4.w};
                         const float fu[4] = {ou4.x, ou4.y, ou4.z, ou4.w};
+                        const float gv[4] = {d4v.x, d4v.y, d4v.z, d4v.w};
+                        const float gw[4] = {d4w.x, d4w.y, d4w.z, d4w.w};
+                        const float gu[4] = {d4u.x, d4u.y, d4u.z, d4u.w};
 #pragma unroll
                         for (int m = 0; m < 4; ++m)
                             if (stored(j + m)) {
                                 __stcg(a.vo + goff + m, fv[m]);
                                 __stcg(a.wo + goff + m, fw[m]);
                                 __stcg(a.uo + goff + m, fu[m]);
+                                if (HEUN == 1) {
+                                    __stcg(a.dso + goff + m, gv[m]);
+                                    __stcg(a.dso + pl + goff + m, gw[m]);
+                                    __stcg(a.dso + 2 * pl + goff + m, gu[m]);
+                                }
                             }
                     }
                 }
@@ -719,7 +767,9 @@ __device__ __forceinline__ bool is_sliver(int i0, int j0, int H, int W) {
 // Interior tiles, clamped edge tiles, or slivers (interior passes + per-cell band).
 // PK: packed arithmetic with the launch's constants *pk (null when !PK).
 // DIRECT: see compute_tile; returns false when the tile was abandoned (a failed TMA wait).
-template <bool DERIV, bool ACT, bool PK = false, bool DIRECT = false, class P1, class P2 = NoHook>
+// HEUN: 1 or 2 for the Heun stages (PK and DIRECT only).
+template <bool DERIV, bool ACT, bool PK = false, bool DIRECT = false, int HEUN = 0, class P1,
+          class P2 = NoHook>
 __device__ __forceinline__ bool process_tile(const StepArgs &a, float t, const Stage &st,
                                              float *sux, float *suy, const TileIO &io,
                                              unsigned active, int i0, int j0, P1 &&after_pass1,
@@ -728,18 +778,21 @@ __device__ __forceinline__ bool process_tile(const StepArgs &a, float t, const S
     const int H = a.H, W = a.W;
     const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
     if (interior) {
-        return compute_tile<DERIV, ACT, false, PK, DIRECT>(a, pk, t, st, sux, suy, io, active, i0,
-                                                           j0, after_pass1, ok, after_barrier);
+        return compute_tile<DERIV, ACT, false, PK, DIRECT, HEUN>(a, pk, t, st, sux, suy, io, active,
+                                                                 i0, j0, after_pass1, ok,
+                                                                 after_barrier);
     } else if (!is_sliver(i0, j0, H, W)) {
-        return compute_tile<DERIV, ACT, true, PK, DIRECT>(a, pk, t, st, sux, suy, io, active, i0,
-                                                          j0, after_pass1, ok, after_barrier);
+        return compute_tile<DERIV, ACT, true, PK, DIRECT, HEUN>(a, pk, t, st, sux, suy, io, active,
+                                                                i0, j0, after_pass1, ok,
+                                                                after_barrier);
     } else if (DIRECT) {
         // interior cells from the tile passes; the band cells per cell, straight to global memory
-        if (!compute_tile<DERIV, ACT, false, PK, DIRECT>(a, pk, t, st, sux, suy, io, active, i0,
-                                                         j0, after_pass1, ok, after_barrier, true))
+        if (!compute_tile<DERIV, ACT, false, PK, DIRECT, HEUN>(a, pk, t, st, sux, suy, io, active,
+                                                               i0, j0, after_pass1, ok,
+                                                               after_barrier, true))
             return false;
         boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0,
-                                     OutTile{nullptr, nullptr, nullptr, i0, j0});
+                                     OutTile{nullptr, nullptr, nullptr, i0, j0}, HEUN);
         return true;
     } else {
         compute_tile<DERIV, false, false, PK>(a, pk, t, st, sux, suy, io, active, i0, j0,
