@@ -351,7 +351,10 @@ constexpr int AYW = ATX + 4;  // row width of the y-derivative planes (tile colu
 // Tile (bx, by) of the step described by `a` (a kernel parameter, or a block's shared copy);
 // its dL/dtheta partial sums go to slot by * nbx + bx of a.gtheta.
 __device__ __forceinline__ void adjoint_tile(const AdjointArgs &a, int bx, int by, int nbx) {
-    __shared__ float su[ASH * ASW], sd[ASH * ASW], sm[ASH * ASW];  // u, D, mu = dt lam'_u
+    // u, D, mu = dt lam'_u (16-byte aligned: filled with float4 stores when the halo is in-grid)
+    __shared__ __align__(16) float su[ASH * ASW];
+    __shared__ __align__(16) float sd[ASH * ASW];
+    __shared__ __align__(16) float sm[ASH * ASW];
     __shared__ float sux[(ATY + 4) * AXW], sqx[(ATY + 4) * AXW], sbx[(ATY + 4) * AXW];
     __shared__ float suy[ATY * AYW], sqy[ATY * AYW], sby[ATY * AYW];
     __shared__ float red[kAdjParams][ANT / 32];
@@ -373,13 +376,29 @@ __device__ __forceinline__ void adjoint_tile(const AdjointArgs &a, int bx, int b
 
     // u, D, mu with a 4-cell halo; out-of-grid positions hold clamped copies, read only by
     // cells that take the explicit path along that axis
-    for (int k = tid; k < ASH * ASW; k += ANT) {
-        const int r = k / ASW, c = k % ASW;
-        const int64_t g = (int64_t)clampi(i0 - AHALO + r, 0, H - 1) * pitch +
-                          clampi(j0 - AHALO + c, 0, W - 1);
-        su[k] = __ldg(a.u + g);
-        sd[k] = __ldg(a.D + g);
-        sm[k] = dt * __ldg(a.lu + g);
+    if (i0 >= AHALO && i0 + ATY + AHALO <= H && j0 >= AHALO && j0 + ATX + AHALO <= W) {
+        // halo inside the grid: 16-byte loads (rows start at column j0 - 4, a multiple of 4)
+        constexpr int SW4 = ASW / 4;
+        for (int k = tid; k < ASH * SW4; k += ANT) {
+            const int r = k / SW4, c4 = k % SW4;
+            const int64_t g = (int64_t)(i0 - AHALO + r) * pitch + j0 - AHALO + 4 * c4;
+            const float4 u4 = __ldg(reinterpret_cast<const float4 *>(a.u + g));
+            const float4 d4 = __ldg(reinterpret_cast<const float4 *>(a.D + g));
+            const float4 l4 = __ldg(reinterpret_cast<const float4 *>(a.lu + g));
+            reinterpret_cast<float4 *>(su)[k] = u4;
+            reinterpret_cast<float4 *>(sd)[k] = d4;
+            reinterpret_cast<float4 *>(sm)[k] =
+                make_float4(dt * l4.x, dt * l4.y, dt * l4.z, dt * l4.w);
+        }
+    } else {
+        for (int k = tid; k < ASH * ASW; k += ANT) {
+            const int r = k / ASW, c = k % ASW;
+            const int64_t g = (int64_t)clampi(i0 - AHALO + r, 0, H - 1) * pitch +
+                              clampi(j0 - AHALO + c, 0, W - 1);
+            su[k] = __ldg(a.u + g);
+            sd[k] = __ldg(a.D + g);
+            sm[k] = dt * __ldg(a.lu + g);
+        }
     }
     __syncthreads();
     // edge-band line products from the shared halo (edge tiles only)
