@@ -8,9 +8,10 @@ the GPU, so nothing leaves the device until the caller reads the result.
 
 Like the reference's ``states`` dataset, the result has ``len(checkpoints)`` rows of which the
 first ``len(checkpoints) - 1`` are written (row i: the state at ``checkpoints[i + 1]``) and the
-last stays zero.  With ``filename`` the data set is also written (``io.save``: the reference's
-HDF5 dataset names in a ``.npz`` archive).  Plotting and progress printing are not part of this
-package.
+last stays zero.  With ``filename`` the data set is also written as the reference writes it
+(``io.init``, ``add_params``, ``add_stimuli``, ``add_diffusivity`` at the output shape, then
+the states: row by row as they are computed, or all at the end with ``use_memory``).
+Plotting and progress printing are not part of this package.
 """
 from __future__ import annotations
 
@@ -37,10 +38,21 @@ def sequence(start: int, stop: int, step: int, dt: float, dx: float, params, dif
     tis = Tissue(shape, params, diffusivity, stimuli, dt=dt, dx=dx, device=device)
     n = len(checkpoints)
     states = torch.zeros((n, 3) + out_shape, dtype=torch.float32, device=tis.device)
-    for i in range(n - 1):
-        tis.advance(checkpoints[i], checkpoints[i + 1])
-        io.resize_planes(tis.state, tis.H, tis.W, states[i], antialias)
+    hdf5 = None
     if filename is not None:
-        io.save(filename, states, params, diffusivity, stimuli, dt, dx,
-                shape=out_shape if reshape is not None else None)
+        hdf5 = io.init(filename, out_shape, n_iter=n, n_stimuli=len(stimuli))
+        io.add_params(hdf5, params, diffusivity, dt, dx, shape=out_shape)
+        io.add_stimuli(hdf5, stimuli, shape=out_shape)
+        io.add_diffusivity(hdf5, diffusivity, shape=out_shape)
+    try:
+        for i in range(n - 1):
+            tis.advance(checkpoints[i], checkpoints[i + 1])
+            io.resize_planes(tis.state, tis.H, tis.W, states[i], antialias)
+            if hdf5 is not None and not use_memory:
+                io.add_state(hdf5["states"], states[i], i)
+        if hdf5 is not None and use_memory and n > 1:
+            io.add_states(hdf5["states"], states[:n - 1], 0, n - 1)
+    finally:
+        if hdf5 is not None:
+            hdf5.close()
     return states

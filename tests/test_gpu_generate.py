@@ -74,10 +74,36 @@ def test_sequence_matches_oracle(tmp_path):
         ref = O.imresize_bilinear(np.stack(st), (32, 40))
         assert np.abs(states[i].cpu().numpy() - ref).max() <= 1e-4
     assert float(states[3].abs().max()) == 0.0  # the last row is never written
-    data = io.load(str(tmp_path / "seq.npz"))
-    assert data["states"].shape == (4, 3, 32, 40)
-    assert data["diffusivity"].shape == (32, 40) and data["field"].shape == (1, 32, 40)
-    assert float(data["params/tau_d"]) == 0.25 and float(data["params/dt"]) == 0.01
+    from cardiax_gb300 import h5
+    with h5.File(str(tmp_path / "seq")) as data:
+        assert np.array_equal(data["states"][:], states.cpu().numpy())
+        assert data["diffusivity"].shape == (32, 40) and data["field"].shape == (1, 32, 40)
+        assert data["stimuli"].shape == (1, 32, 40)
+        assert np.array_equal(data["params/D"][:], data["diffusivity"][:])
+        ref_field = O.imresize_bilinear(f[None], (32, 40))[0]
+        assert np.abs(data["field"][0] - ref_field).max() <= 2e-6 * 20.0
+        assert float(data["params/tau_d"][()]) == 0.25 and float(data["params/dt"][()]) == 0.01
+        assert list(data["period"][:]) == [1e9]
+    params, D2 = io.load_params(str(tmp_path / "seq"))
+    assert tuple(params) == P3 and D2.shape == (32, 40)
+
+
+def test_sequence_streams_rows_to_the_file(tmp_path):
+    """use_memory=False: each state is written as it is computed (deepx/generate.py:199-200)."""
+    _gpu()
+    from cardiax_gb300 import generate, h5
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    H, W = 48, 40
+    D = np.full((H, W), 1e-3, np.float32)
+    f = np.zeros((H, W), np.float32)
+    f[:4, :] = 20.0
+    stims = [Stimulus(Protocol(0, 2, 1e9), f)]
+    path = str(tmp_path / "out" / "rows.hdf5")
+    states = generate.sequence(0, 250, 50, 0.01, 0.01, P3, D, stims, filename=path,
+                               use_memory=False)
+    with h5.File(path) as data:
+        assert np.array_equal(data["states"][:], states.cpu().numpy())
+        assert np.array_equal(data["diffusivity"][:], D)
 
 
 @pytest.mark.parametrize("shape,angle", [((64, 80), 30.0), ((50, 33), -47.5), ((128, 128), 90.0),
