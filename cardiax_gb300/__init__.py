@@ -5,7 +5,7 @@ CUDA kernels behind a C ABI (``include/cardiax_gb300.h``), driven from Python th
 torch CUDA tensors and streams.
 """
 from . import convert, params, stimulus  # noqa: F401
-from . import generate, io, solve  # noqa: F401
+from . import generate, io, scars, solve  # noqa: F401
 from .tissue import Tissue  # noqa: F401
 
-__all__ = ["convert", "generate", "io", "params", "stimulus", "solve", "Tissue"]
+__all__ = ["convert", "generate", "io", "params", "scars", "stimulus", "solve", "Tissue"]

@@ -88,6 +88,8 @@ _SIGNATURES = {
                         _I64, _I64, _D, _D, _P],
     "fk_resize_bilinear": [_P, _I64, _I64, _I64, _I64, _P, _I64, _I64, _I64, _INT, _P],
     "fk_rotate_field": [_P, _I64, _I64, _I64, _P, _I64, _D, _P],
+    "fk_scar_raster": [_P, _P, _P, _I64, _I64, _I64, _P, _I64, _P, _P],
+    "fk_conv2d_same": [_P, _I64, _I64, _I64, _P, _I64, _P, _I64, _INT, _P],
     "fk_batch_create": [ctypes.POINTER(TissueDesc), _INT, _P, ctypes.c_size_t, _P,
                         ctypes.POINTER(_P)],
     "fk_batch_forward_euler": [_P, _I64, _I64, _INT, _P],

@@ -49,6 +49,16 @@ def units_to_ms(value, dt):
     return value * dt
 
 
+def stimuli_to_units(stimuli, dx, dt):
+    """``start``, ``duration`` and ``period`` of each stimulus mapping converted from ms to
+    steps, in place (cardiax/convert.py:53-59)."""
+    stimuli = list(stimuli)
+    for s in stimuli:
+        for key in ("start", "duration", "period"):
+            s[key] = ms_to_units(s[key], dt)
+    return stimuli
+
+
 def u_to_V(u, V0=-85, Vfi=15):
     return ((Vfi - V0) * u) + V0
 

@@ -19,7 +19,7 @@ from typing import Sequence
 
 import torch
 
-from . import io
+from . import convert, io, scars
 from .tissue import Tissue
 
 
@@ -56,3 +56,11 @@ def sequence(start: int, stop: int, step: int, dt: float, dx: float, params, dif
         if hdf5 is not None:
             hdf5.close()
     return states
+
+
+def random_diffusivity(rng, shape: Sequence[int], domain: Sequence[float] = (0.0001, 0.001),
+                       device=None) -> torch.Tensor:
+    """A scar map (``scars.random_diffusivity_scar``) rescaled onto ``domain``
+    (deepx/generate.py:79-83): an (H, W) float32 device tensor."""
+    c = scars.random_diffusivity_scar(rng, shape, device)
+    return convert.diffusivity_rescale(c, domain)

@@ -93,7 +93,10 @@ def add_params(hdf5: h5.Group, params, diffusivity, dt, dx, shape=None) -> bool:
     hdf5.create_dataset("params/D", data=_resized(diffusivity, shape))
     hdf5.create_dataset("params/dt", data=_scalar(dt))
     hdf5.create_dataset("params/dx", data=_scalar(dx))
-    for name, value in zip(type(params)._fields, params):
+    from .params import Params
+
+    names = getattr(type(params), "_fields", Params._fields)  # a plain tuple in Params order
+    for name, value in zip(names, params):
         hdf5.create_dataset("params/" + name, data=_scalar(value))
     return True
 

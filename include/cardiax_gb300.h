@@ -195,6 +195,29 @@ int fk_resize_bilinear(const float *in, int64_t planes, int64_t H, int64_t W, in
 int fk_rotate_field(const float *in, int64_t H, int64_t W, int64_t pitch, float *out,
                     int64_t out_pitch, double angle_deg, void *stream);
 
+/* Scar maps (deepx/utils_scars.py:409-426 random_diffusivity_scar; the polygon outlines, random
+ * draws and Gaussian weights are host work of a few hundred values).
+ *
+ * fk_scar_raster: the H x W plane `out` (pitch) set to 1 where a cell lies inside any of
+ * `n_polys` <= 16 polygons and 0 elsewhere -- the union of skimage.draw.polygon fills of
+ * utils_scars.py:79-97 clipped at 1 (utils_scars.py:356-360).  Polygon p has the vertices
+ * (xs[k], ys[k]) for k in [offsets[p], offsets[p + 1]) (device arrays of doubles, x = column,
+ * y = row; `offsets` is a HOST array of n_polys + 1 ints starting at 0, at least 3 vertices per
+ * polygon, 4096 in all).  A cell (r, c) is inside when PNPOLY's crossing test holds at
+ * (x = c, y = r), in double precision with separately rounded operations.  The number of cells
+ * set is ADDED to *count (a device counter the caller zeroes). */
+int fk_scar_raster(const double *xs, const double *ys, const int32_t *offsets, int64_t n_polys,
+                   int64_t H, int64_t W, float *out, int64_t pitch, unsigned long long *count,
+                   void *stream);
+
+/* fk_conv2d_same: scipy.signal.convolve2d(in, kernel, "same") in float32 (the blur of
+ * utils_scars.py:402-406): out[i][j] = sum over a, b < K of kernel[a * K + b] *
+ * in[i + (K - 1) / 2 - a][j + (K - 1) / 2 - b], zero outside the plane; stored as 1 - out when
+ * `one_minus` (utils_scars.py:426).  `kernel` is a device array of K * K floats; `in` and `out`
+ * are distinct H x W planes (pitches in elements). */
+int fk_conv2d_same(const float *in, int64_t H, int64_t W, int64_t in_pitch, const float *kernel,
+                   int64_t K, float *out, int64_t out_pitch, int one_minus, void *stream);
+
 /* ---- many tissues in one launch --------------------------------------------------------------
  * No reference counterpart: the reference steps one tissue per call (its data generation loops
  * over tissues in Python, deepx/generate.py:135-210).  Here every tissue of a batch advances in
