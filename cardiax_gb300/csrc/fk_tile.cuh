@@ -246,37 +246,47 @@ __device__ __forceinline__ void issue_tile_hinted(const StepMaps &tm, const Stag
     tma_load_2d_hint(st.d, &tm.d, j0 - HALO_U, i0 - HALO_D, bar, pol_d);
 }
 
-// load_vw with an L2 policy (the v, w read here are read for the last time).
-__device__ __forceinline__ void load_vw_hinted(const StepArgs &a, int i0, int j0, TileIO &io,
-                                               uint64_t pol) {
+// A tile lying wholly inside the grid (its loads and stores need no bounds checks).
+__device__ __forceinline__ bool tile_in_grid(int i0, int j0, int H, int W) {
+    return i0 + TY <= H && j0 + TX <= W;
+}
+
+// This thread's v, w for pass 2 (16-byte loads, zero outside the grid), read with `load`.
+template <class Load>
+__device__ __forceinline__ void load_vw_with(const StepArgs &a, int i0, int j0, TileIO &io,
+                                             Load load) {
     const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
     const int j = j0 + 4 * tx;
+    if (tile_in_grid(i0, j0, a.H, a.W)) {
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+            const int64_t off = (int64_t)(i0 + RPT * ty + k) * a.pitch + j;
+            io.v[k] = load(a.v + off);
+            io.w[k] = load(a.w + off);
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
         const int i = i0 + RPT * ty + k;
         io.v[k] = io.w[k] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (i < a.H && j < a.W) {
             const int64_t off = (int64_t)i * a.pitch + j;
-            io.v[k] = ld_f4_hint(a.v + off, pol);
-            io.w[k] = ld_f4_hint(a.w + off, pol);
+            io.v[k] = load(a.v + off);
+            io.w[k] = load(a.w + off);
         }
     }
 }
 
-// This thread's v, w for pass 2 (16-byte loads, zero outside the grid).
+// load_vw with an L2 policy (the v, w read here are read for the last time).
+__device__ __forceinline__ void load_vw_hinted(const StepArgs &a, int i0, int j0, TileIO &io,
+                                               uint64_t pol) {
+    load_vw_with(a, i0, j0, io, [pol](const float *p) { return ld_f4_hint(p, pol); });
+}
+
 __device__ __forceinline__ void load_vw(const StepArgs &a, int i0, int j0, TileIO &io) {
-    const int tx = threadIdx.x % NTX, ty = threadIdx.x / NTX;
-    const int j = j0 + 4 * tx;
-#pragma unroll
-    for (int k = 0; k < RPT; ++k) {
-        const int i = i0 + RPT * ty + k;
-        io.v[k] = io.w[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (i < a.H && j < a.W) {
-            const int64_t off = (int64_t)i * a.pitch + j;
-            io.v[k] = __ldcg(reinterpret_cast<const float4 *>(a.v + off));
-            io.w[k] = __ldcg(reinterpret_cast<const float4 *>(a.w + off));
-        }
-    }
+    load_vw_with(a, i0, j0, io,
+                 [](const float *p) { return __ldcg(reinterpret_cast<const float4 *>(p)); });
 }
 
 // Edge tiles: replace the zero fill of the out-of-grid halo by the reference's edge padding
@@ -449,6 +459,8 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
     }
 
     // ---- pass 2: second derivatives, D terms, reaction, stimulus, Euler update --------------
+    // whole: every cell of the tile is stored (an interior tile: inside the grid, no band)
+    const bool whole = !EDGE && !band_mask;
     const int tx = tid % NTX, ty = tid / NTX;
     const int j = j0 + 4 * tx;
     // PK: the u_x and D rows RPT*ty-2 .. RPT*ty+RPT+1 of this thread's quad, read once for all
@@ -557,7 +569,7 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                 const int64_t pl = (int64_t)H * pitch;
                 const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
                 float4 xv = z, xw = z, xu = z, dv1 = z, dw1 = z, du1 = z;
-                if (i < H && j < W) {
+                if (whole || (i < H && j < W)) {
                     xv = __ldcg(reinterpret_cast<const float4 *>(a.x0 + goff));
                     xw = __ldcg(reinterpret_cast<const float4 *>(a.x0 + pl + goff));
                     xu = __ldcg(reinterpret_cast<const float4 *>(a.x0 + 2 * pl + goff));
@@ -589,13 +601,13 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                                                  jj >= W - BAND));
             };
             if constexpr (DIRECT) {
-                if (i < H && j < W) {
+                if (whole || (i < H && j < W)) {
                     const int64_t pl = (int64_t)H * pitch;
                     // Heun stage 1 also stores d1 (the derivative at the input state)
                     const float4 d4v = make_float4(rl.dv.x, rl.dv.y, rh.dv.x, rh.dv.y);
                     const float4 d4w = make_float4(rl.dw.x, rl.dw.y, rh.dw.x, rh.dw.y);
                     const float4 d4u = make_float4(du_lo.x, du_lo.y, du_hi.x, du_hi.y);
-                    if (!band_mask && j + 3 < W) {
+                    if (whole || (!band_mask && j + 3 < W)) {
                         __stcg(reinterpret_cast<float4 *>(a.vo + goff), ov4);
                         __stcg(reinterpret_cast<float4 *>(a.wo + goff), ow4);
                         __stcg(reinterpret_cast<float4 *>(a.uo + goff), ou4);
@@ -729,8 +741,8 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                                              jj >= W - BAND));
         };
         if constexpr (DIRECT) {
-            if (i < H && j < W) {
-                if (!band_mask && j + 3 < W) {
+            if (whole || (i < H && j < W)) {
+                if (whole || (!band_mask && j + 3 < W)) {
                     __stcg(reinterpret_cast<float4 *>(a.vo + goff), make_float4(ov[0], ov[1], ov[2], ov[3]));
                     __stcg(reinterpret_cast<float4 *>(a.wo + goff), make_float4(ow[0], ow[1], ow[2], ow[3]));
                     __stcg(reinterpret_cast<float4 *>(a.uo + goff), make_float4(ou[0], ou[1], ou[2], ou[3]));
