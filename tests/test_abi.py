@@ -64,3 +64,25 @@ def test_null_and_argument_checks():
     assert L.fk_forward_euler(g, 16, 32, 48, ctypes.byref(p), s, 9, 0, 1, 0.01, 0.01, None) == 4
     ck = (ctypes.c_int64 * 3)(0, 5, 3)
     assert L.fk_forward(g, 16, 32, 48, ctypes.byref(p), s, 0, ck, 3, 0.01, 0.01, 64, None) == 5
+
+
+def test_scar_entry_points_check_arguments():
+    """fk_scar_raster / fk_conv2d_same reject bad arguments before any device work."""
+    from cardiax_gb300 import _native as N
+    L = N.lib()
+    off = (ctypes.c_int32 * 3)(0, 5, 10)
+    fake = 0x1000  # never dereferenced: each call below fails its host-side checks first
+    assert L.fk_scar_raster(fake, fake, off, 2, 16, 16, None, 16, fake, None) == 1
+    assert L.fk_scar_raster(fake, fake, None, 2, 16, 16, fake, 16, fake, None) == 1
+    assert L.fk_scar_raster(fake, fake, off, 17, 16, 16, fake, 16, fake, None) == 2
+    assert L.fk_scar_raster(fake, fake, off, 2, 16, 16, fake, 8, fake, None) == 2
+    bad0 = (ctypes.c_int32 * 2)(1, 5)
+    assert L.fk_scar_raster(fake, fake, bad0, 1, 16, 16, fake, 16, fake, None) == 5
+    short = (ctypes.c_int32 * 3)(0, 5, 7)  # a polygon of two vertices
+    assert L.fk_scar_raster(fake, fake, short, 2, 16, 16, fake, 16, fake, None) == 5
+    big = (ctypes.c_int32 * 2)(0, 5000)
+    assert L.fk_scar_raster(fake, fake, big, 1, 16, 16, fake, 16, fake, None) == 5
+    assert L.fk_conv2d_same(None, 8, 8, 8, fake, 3, fake + 64, 8, 0, None) == 1
+    assert L.fk_conv2d_same(fake, 8, 8, 8, fake, 0, fake + 64, 8, 0, None) == 2
+    assert L.fk_conv2d_same(fake, 8, 8, 4, fake, 3, fake + 64, 8, 0, None) == 2
+    assert L.fk_conv2d_same(fake, 8, 8, 8, fake, 3, fake, 8, 0, None) == 5
