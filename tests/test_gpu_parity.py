@@ -16,7 +16,7 @@ import fk_oracle as O
 pytestmark = pytest.mark.gpu
 
 P3 = (3.33, 19.6, 1250, 870, 41, 0.25, 12.5, 33.33, 29, 10, 0.85, 0.13, 0.04, 1)
-TOL_U_1000 = 1e-4   # pointwise max|du| after 1000 steps (spec bar)
+TOL_U_1000 = 1e-4   # pointwise max|du| after 1000 steps (the stated parity bar)
 
 
 def _gpu():
