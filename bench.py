@@ -289,6 +289,24 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The largest ``x`` over the ranks of the default process group (``x`` itself without
+    one): each replica's time, so that the whole-job figure is set by the slowest replica."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_gcups(updates_per_rank: float, seconds: float, world: int) -> float:
+    """Whole-job GCUPS of ``world`` independent replicas that each made ``updates_per_rank``
+    cell updates in at most ``seconds`` (the max over ranks)."""
+    return world * updates_per_rank / seconds / 1e9
+
+
 def cpu_port_rate(H, W, D, field, proto, seconds: float, threads: int):
     """GCUPS of the C oracle on a bounded sample (steps chosen to take about ``seconds``)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -492,13 +510,8 @@ def run_ours(args):
         dist.barrier()
     t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
-    ms = sum(a.elapsed_time(b) for a, b in evs)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    updates = world * args.steps * H * W * S
-    value = updates / (ms / 1e3) / 1e9
+    ms = max_over_ranks(sum(a.elapsed_time(b) for a, b in evs), dev)
+    value = replica_gcups(args.steps * H * W * S, ms / 1e3, world)
 
     # end to end through the public API from pinned host memory
     e2e = None
@@ -519,12 +532,8 @@ def run_ours(args):
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
             del states, host
-        e2e_s = sum(times)
-        if world > 1:
-            t = torch.tensor([e2e_s], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": world * len(times) * H * W * S / e2e_s / 1e9, "unit": "GCUPS",
+        e2e_s = max_over_ranks(sum(times), dev)
+        e2e = {"value": replica_gcups(len(times) * H * W * S, e2e_s, world), "unit": "GCUPS",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     peak, peak_kind = peaks()
