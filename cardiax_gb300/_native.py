@@ -63,6 +63,7 @@ _INT = ctypes.c_int
 _SIGNATURES = {
     "fk_device_status": [_INT, ctypes.POINTER(_INT)],
     "fk_select_step_kernel": [_INT],
+    "fk_selftest_wait_timeout": [_I64, _P],
     "fk_init": [Grid, _P, _P],
     "fk_step": [Grid, _P, _P, ctypes.POINTER(Params), ctypes.POINTER(Stimulus), _INT, _I64, _D,
                 _P, _P],

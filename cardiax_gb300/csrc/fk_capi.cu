@@ -24,6 +24,7 @@
 
 #include "../../include/cardiax_gb300.h"
 #include "fk_capi_internal.h"
+#include "fk_ptx.cuh"
 #include "fk_adjoint.cuh"
 #include "fk_step.cuh"
 #include "fk_strip.cuh"
@@ -391,6 +392,28 @@ int fk_device_status(int reset, int *value) {
     if (cudaMemcpy(value, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return FK_ERR_CUDA;
     if (reset && cudaMemset(p, 0, sizeof(int)) != cudaSuccess) return FK_ERR_CUDA;
     return FK_OK;
+}
+
+namespace fk {
+namespace {
+// One warp whose thread 0 waits on an mbarrier that nothing arrives on: the bounded wait of the
+// step kernels runs out after `limit_ns` and the kernel reports it as they do.
+__global__ void selftest_wait_kernel(uint64_t limit_ns, int *status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+    if (!mbar_wait_bounded(&bar, 0, limit_ns)) atomicOr(status, kStatusTimeout);
+}
+}  // namespace
+}  // namespace fk
+
+int fk_selftest_wait_timeout(int64_t limit_ns, void *stream) {
+    if (limit_ns < 1000 || limit_ns > 2000000000ll) return FK_ERR_ARGUMENT;
+    int *st = fk::status_ptr();
+    if (!st) return FK_ERR_CUDA;
+    fk::selftest_wait_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((uint64_t)limit_ns, st);
+    return cudaGetLastError() == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
 
 int fk_init(fk_grid g, float *state, void *stream) {

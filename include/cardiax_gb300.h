@@ -73,6 +73,12 @@ const char *fk_status_string(int status);
 /* Reads (and with reset != 0 clears) the device error word of the current device. */
 int fk_device_status(int reset, int *value);
 
+/* Failure-path self-test: launches one warp that waits on a barrier nothing completes, with the
+ * bounded wait the step kernels use cut to `limit_ns` (1 us .. 2 s); when it runs out the kernel
+ * sets the device error word (read it with fk_device_status) and returns, leaving the context
+ * usable.  No counterpart in the reference. */
+int fk_selftest_wait_timeout(int64_t limit_ns, void *stream);
+
 /* Which kernel takes the Euler steps of every single-tissue entry point (process-wide):
  * 0 = the tiled kernel (32 x 64-cell tiles, two passes) -- the default; 1 = the strip kernel
  * (128-column strips walked row by row with register windows) wherever it applies (W % 128 != 1),

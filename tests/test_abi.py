@@ -86,3 +86,10 @@ def test_scar_entry_points_check_arguments():
     assert L.fk_conv2d_same(fake, 8, 8, 8, fake, 0, fake + 64, 8, 0, None) == 2
     assert L.fk_conv2d_same(fake, 8, 8, 4, fake, 3, fake + 64, 8, 0, None) == 2
     assert L.fk_conv2d_same(fake, 8, 8, 8, fake, 3, fake, 8, 0, None) == 5
+
+
+def test_selftest_wait_timeout_checks_its_limit():
+    from cardiax_gb300 import _native as N
+    L = N.lib()
+    assert L.fk_selftest_wait_timeout(10, None) == 5
+    assert L.fk_selftest_wait_timeout(3_000_000_000, None) == 5
