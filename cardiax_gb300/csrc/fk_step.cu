@@ -74,11 +74,10 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
     TileIO io;
     io.ov = io.ow = io.ou = nullptr;
     uint64_t *bar = reinterpret_cast<uint64_t *>(suy + 2 * SW * TY);            // [NSTAGE]
-    StepArgs *sa = reinterpret_cast<StepArgs *>(bar + NSTAGE);
+    // the arguments are read in place (a __grid_constant__ parameter: constant-bank operands)
 
     const int tid = threadIdx.x;
     const int ntx = (a.W + TX - 1) / TX, nty = (a.H + TY - 1) / TY, ntiles = ntx * nty;
-    stage_args(sa, &a);
     if (tid == 0) {
         prefetch_tensormap(&tm.u);
         prefetch_tensormap(&tm.d);
@@ -126,9 +125,9 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
         const int s = n % NSTAGE;
         const int i0 = tile_i0(tile), j0 = tile_j0(tile);
         if (hints)
-            load_vw_hinted(*sa, i0, j0, io, pol_dead);
+            load_vw_hinted(a, i0, j0, io, pol_dead);
         else
-            load_vw(*sa, i0, j0, io);
+            load_vw(a, i0, j0, io);
         const bool ok = mbar_wait_bounded(&bar[s], (n / NSTAGE) & 1);
         // after the barrier between this tile's passes every thread has finished tile n-1, so
         // its stage takes tile n+2
@@ -137,7 +136,7 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
             if (tid == 0 && ahead < ntiles) issue(ahead, (n + NSTAGE - 1) % NSTAGE);
         };
         float *ux_n = sux + (n & 1) * (TX * SUX_H), *uy_n = suy + (n & 1) * (SW * TY);
-        if (!process_tile<DERIV, ACT, true, true, HEUN>(*sa, a.t, stage_at(smem, s), ux_n, uy_n,
+        if (!process_tile<DERIV, ACT, true, true, HEUN>(a, a.t, stage_at(smem, s), ux_n, uy_n,
                                                         io, active, i0, j0, NoHook{}, &k, ok,
                                                         refill)) {
             if (tid == 0) atomicOr(a.status, kStatusTimeout);
