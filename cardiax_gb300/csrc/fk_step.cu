@@ -89,15 +89,10 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
     grid_dependency_wait();
     grid_launch_dependents();
     const TileOrder order(a.H, a.W);
-    auto tile_i0 = [&](int tl) {
+    auto tile_at = [&](int tl) {  // (i0, j0) of the tl-th tile handed out
         int tr, tc;
         order.at(tl, tr, tc);
-        return tr * TY;
-    };
-    auto tile_j0 = [&](int tl) {
-        int tr, tc;
-        order.at(tl, tr, tc);
-        return tc * TX;
+        return make_int2(tr * TY, tc * TX);
     };
     int tile = blockIdx.x;
     // L2 policies: the input state is read for the last time (the next step overwrites its
@@ -105,11 +100,11 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
     const bool hints = a.l2_hints != 0;
     const uint64_t pol_dead = l2_policy_evict_first(), pol_keep = l2_policy_evict_last();
     auto issue = [&](int tl, int s) {
+        const int2 ij = tile_at(tl);
         if (hints)
-            issue_tile_hinted(tm, stage_at(smem, s), &bar[s], tile_i0(tl), tile_j0(tl), pol_dead,
-                              pol_keep);
+            issue_tile_hinted(tm, stage_at(smem, s), &bar[s], ij.x, ij.y, pol_dead, pol_keep);
         else
-            issue_tile(tm, stage_at(smem, s), &bar[s], tile_i0(tl), tile_j0(tl));
+            issue_tile(tm, stage_at(smem, s), &bar[s], ij.x, ij.y);
     };
     if (tid == 0)  // prologue: the first two tiles of this CTA
         for (int q = 0; q < NSTAGE - 1; ++q) {
@@ -123,7 +118,8 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
 
     for (int n = 0; tile < ntiles; ++n, tile += gridDim.x) {
         const int s = n % NSTAGE;
-        const int i0 = tile_i0(tile), j0 = tile_j0(tile);
+        const int2 ij = tile_at(tile);
+        const int i0 = ij.x, j0 = ij.y;
         if (hints)
             load_vw_hinted(a, i0, j0, io, pol_dead);
         else
