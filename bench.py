@@ -416,17 +416,19 @@ def run_next_rows(dev, reps: int = 2):
     return {"heun": heun_r, "sequence": seq_r}
 
 
-def run_schedules(dev, sizes=(1024, 2048), steps: int = 400):
+def run_schedules(dev, sizes=(256, 512, 1024, 2048), steps: int = 400):
     """GCUPS of each stepping schedule on the roofline workload (best of 2 runs of ``steps``
-    steps, L2 flushed before each run)."""
+    steps, L2 flushed before each run), and of ``schedule="auto"`` with the choice the tissue
+    autotuner made."""
     import torch
     from cardiax_gb300 import params
     from cardiax_gb300.stimulus import Protocol, Stimulus
     from cardiax_gb300.tissue import Tissue
 
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    from cardiax_gb300 import autotune
     modes = {"k1": {}, "k2": {"depth": 2}, "k4": {"depth": 4}, "k8": {"depth": 8},
-             "flow": {"schedule": "flow"}}
+             "flow": {"schedule": "flow"}, "auto": {"schedule": "auto"}}
     out = {}
     for size in sizes:
         D, field, proto = workload(size, size)
@@ -448,6 +450,10 @@ def run_schedules(dev, sizes=(1024, 2048), steps: int = 400):
                 best = ms if best is None else min(best, ms)
             row[name] = {"gcups": size * size * steps / (best / 1e3) / 1e9,
                          "us_per_step": best * 1e3 / steps}
+            if name == "auto":
+                sched, depth, kernel = autotune.tune_tissue(tis)["choice"]
+                row[name]["choice"] = {"schedule": sched, "depth": depth,
+                                       "kernel": "strip" if kernel else "tiled"}
         out[f"{size}x{size}"] = row
     return out
 

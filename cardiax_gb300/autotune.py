@@ -1,17 +1,31 @@
-"""Autotuner of the stepping configuration.
+"""Autotuners of the stepping configuration.
 
-For a batch it times, on the batch's own tissues, every candidate of
-(graph_steps ∈ {0, 16, 64, 256}) × (persistent CTAs per SM ∈ {1}) over a short run of steps with
-CUDA events and keeps the fastest; the tissues are restored to their initial state afterwards.
-Choices are cached per (device name, batch signature) for the process.
+``tune_batch``: for a batch, times on the batch's own tissues every ``graph_steps`` candidate
+in {0, 16, 64, 256} (how many steps one captured CUDA graph replays) over a short run with CUDA
+events and keeps the fastest.
+
+``tune_tissue``: for one tissue, times every way of taking its Euler steps -- the tiled step
+kernel (32 x 64-cell tiles), the strip kernel (128-column strips walked row by row), the
+temporally blocked kernel at depth k in {2, 4, 8} (k steps per launch), and the dataflow
+schedule -- on the tissue's own grid, and keeps the fastest.  All of them produce the same bits,
+so the choice changes only the speed (``Tissue.advance(..., schedule="auto")``).
+
+Both restore the timed state afterwards and cache their choice per (device name, shapes) for the
+process.
 """
 from __future__ import annotations
 
 import torch
 
+from . import _native as N
 from .batch import TissueBatch
 
 _CACHE: dict = {}
+_TISSUE_CACHE: dict = {}
+
+# (schedule, depth, step kernel) candidates of tune_tissue; step kernel 0 = tiled, 1 = strip
+TISSUE_CANDIDATES = (("step", 1, 0), ("step", 1, 1), ("step", 2, 0), ("step", 4, 0),
+                     ("step", 8, 0), ("flow", 1, 0))
 
 GRAPH_CANDIDATES = (0, 16, 64, 256)
 
@@ -55,4 +69,60 @@ def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CAND
     batch.graph_steps = best
     res = {"graph_steps": best, "ms_per_step": timings}
     _CACHE[key] = res
+    return res
+
+
+def _run(tis, t0: int, t1: int, choice) -> None:
+    schedule, depth, kernel = choice
+    if kernel:
+        N.call("fk_select_step_kernel", int(kernel))
+    try:
+        if schedule == "flow":
+            tis.advance(t0, t1, schedule="flow")
+        else:
+            tis.advance(t0, t1, schedule="step", depth=depth)
+    finally:
+        if kernel:
+            N.call("fk_select_step_kernel", 0)
+
+
+def tune_tissue(tis, trial_steps: int = 64, candidates=TISSUE_CANDIDATES,
+                verbose: bool = False) -> dict:
+    """The fastest way to step ``tis`` (a :class:`~cardiax_gb300.tissue.Tissue`): returns
+    ``{"choice": (schedule, depth, step_kernel), "us_per_step": {choice: us}}``; the tissue's
+    state is restored.  With activation tracking on, only one-step-per-launch candidates
+    qualify (temporal blocking does not track activations)."""
+    tracking = tis.activation is not None
+    cands = tuple(c for c in candidates if not (tracking and c[1] != 1))
+    key = (torch.cuda.get_device_name(tis.device), tis.H, tis.W, tracking, trial_steps, cands)
+    if key in _TISSUE_CACHE:
+        return _TISSUE_CACHE[key]
+    saved = tis.state.clone()
+    saved_act = None if not tracking else (tis.act_first.clone(), tis.act_last.clone(),
+                                           tis.act_count.clone())
+    timings = {}
+    try:
+        for c in cands:
+            try:
+                _run(tis, 0, 8, c)  # warm-up: kernel attributes, descriptors
+            except N.FkError:
+                continue  # a schedule that does not take this grid
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _run(tis, 8, 8 + trial_steps, c)
+            e1.record()
+            torch.cuda.synchronize()
+            timings[c] = e0.elapsed_time(e1) * 1e3 / trial_steps
+            if verbose:
+                print(f"autotune {c}: {timings[c]:.2f} us/step")
+    finally:
+        tis.state.copy_(saved)
+        if saved_act is not None:
+            tis.act_first.copy_(saved_act[0])
+            tis.act_last.copy_(saved_act[1])
+            tis.act_count.copy_(saved_act[2])
+    best = min(timings, key=timings.get)
+    res = {"choice": best, "us_per_step": timings}
+    _TISSUE_CACHE[key] = res
     return res

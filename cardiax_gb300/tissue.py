@@ -184,7 +184,13 @@ class Tissue:
         """Steps t0 .. t1-1 in place (cardiax/solve.py:92-100).  ``schedule="step"``: one launch
         per step (chained with programmatic dependent launch), or with ``depth`` 2, 4 or 8 that
         many steps per launch (temporal blocking); ``"flow"``: one cooperative dataflow launch
-        for the whole range.  All give identical results."""
+        for the whole range; ``"auto"``: whichever of these (and of the tiled and strip step
+        kernels) ``autotune.tune_tissue`` measured fastest on this grid.  All give identical
+        results."""
+        if schedule == "auto":
+            from . import autotune
+            autotune._run(self, t0, t1, autotune.tune_tissue(self)["choice"])
+            return self
         act = ctypes.byref(self.activation) if self.activation is not None else None
         if schedule == "step" and depth != 1:
             if act is not None:
