@@ -136,6 +136,20 @@ __device__ __forceinline__ float2 pg_tail(const PackConsts &k, float2 a0, float2
     return p_fma(k.c_tail3, a3, s);
 }
 
+// pg_central over the pairs (a0, a1), (a1, a2), (a3, a4), (a4, a5) -- the central stencil of two
+// neighbouring cells along a row -- when only (a0, a1) and (a4, a5) sit in register-aligned pairs:
+// the two middle taps as scalar fmas, the same operations per lane in the same order, so no
+// register moves are needed to form the misaligned pairs.
+__device__ __forceinline__ float2 pg_central_row(const PackConsts &k, float a0, float a1, float a2,
+                                                 float a3, float a4, float a5) {
+    float2 s = p_mul(k.c_1_12, mk2(a0, a1));
+    s.x = fmaf(k.c_m2_3.x, a1, s.x);
+    s.y = fmaf(k.c_m2_3.x, a2, s.y);
+    s.x = fmaf(k.c_2_3.x, a3, s.x);
+    s.y = fmaf(k.c_2_3.x, a4, s.y);
+    return p_fma(k.c_m1_12, mk2(a4, a5), s);
+}
+
 // A quad of 4 consecutive columns held as two pairs (c, c+1) and (c+2, c+3).
 struct Quad {
     float2 lo, hi;

@@ -414,10 +414,8 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
         float o[4];
         if constexpr (PK) {
             const PackConsts &kc = *pk;  // u_y at columns c .. c+3 as the pairs (c, c+1), (c+2, c+3)
-            const float2 lo = p_mul(pg_central(kc, mk2(e[2], e[3]), mk2(e[3], e[4]),
-                                               mk2(e[5], e[6]), mk2(e[6], e[7])), kc.rdx);
-            const float2 hi = p_mul(pg_central(kc, mk2(e[4], e[5]), mk2(e[5], e[6]),
-                                               mk2(e[7], e[8]), mk2(e[8], e[9])), kc.rdx);
+            const float2 lo = p_mul(pg_central_row(kc, e[2], e[3], e[4], e[5], e[6], e[7]), kc.rdx);
+            const float2 hi = p_mul(pg_central_row(kc, e[4], e[5], e[6], e[7], e[8], e[9]), kc.rdx);
             o[0] = lo.x;
             o[1] = lo.y;
             o[2] = hi.x;
@@ -508,14 +506,10 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                                  y2.x, y2.y, y2.z, y2.w};  // u_y at columns j-4 .. j+7
             const float g[12] = {dl.x, dl.y, dl.z, dl.w, dcq.lo.x, dcq.lo.y, dcq.hi.x, dcq.hi.y,
                                  dr.x, dr.y, dr.z, dr.w};  // D at columns j-4 .. j+7
-            float2 uyy_lo = p_mul(pg_central(kc, mk2(f[2], f[3]), mk2(f[3], f[4]), mk2(f[5], f[6]),
-                                             mk2(f[6], f[7])), kc.rdx);
-            float2 uyy_hi = p_mul(pg_central(kc, mk2(f[4], f[5]), mk2(f[5], f[6]), mk2(f[7], f[8]),
-                                             mk2(f[8], f[9])), kc.rdx);
-            float2 dyD_lo = p_mul(pg_central(kc, mk2(g[2], g[3]), mk2(g[3], g[4]), mk2(g[5], g[6]),
-                                             mk2(g[6], g[7])), kc.rdx);
-            float2 dyD_hi = p_mul(pg_central(kc, mk2(g[4], g[5]), mk2(g[5], g[6]), mk2(g[7], g[8]),
-                                             mk2(g[8], g[9])), kc.rdx);
+            float2 uyy_lo = p_mul(pg_central_row(kc, f[2], f[3], f[4], f[5], f[6], f[7]), kc.rdx);
+            float2 uyy_hi = p_mul(pg_central_row(kc, f[4], f[5], f[6], f[7], f[8], f[9]), kc.rdx);
+            float2 dyD_lo = p_mul(pg_central_row(kc, g[2], g[3], g[4], g[5], g[6], g[7]), kc.rdx);
+            float2 dyD_hi = p_mul(pg_central_row(kc, g[4], g[5], g[6], g[7], g[8], g[9]), kc.rdx);
             if (EDGE && (j == 0 || (j <= W - 1 && W - 1 <= j + 3))) {
                 // the one-sided rows at column 0 (head) and W-1 (tail), second derivative / D_y
                 float uy4[4] = {uyy_lo.x, uyy_lo.y, uyy_hi.x, uyy_hi.y};
