@@ -107,13 +107,19 @@ def tune_tissue(tis, trial_steps: int = 64, candidates=TISSUE_CANDIDATES,
                 _run(tis, 0, 8, c)  # warm-up: kernel attributes, descriptors
             except N.FkError:
                 continue  # a schedule that does not take this grid
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            _run(tis, 8, 8 + trial_steps, c)
-            e1.record()
-            torch.cuda.synchronize()
-            timings[c] = e0.elapsed_time(e1) * 1e3 / trial_steps
+            best = None
+            for rep in range(2):  # the better of two runs
+                t0 = 8 + rep * trial_steps
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                _run(tis, t0, t0 + trial_steps, c)
+                e1.record()
+                torch.cuda.synchronize()
+                us = e0.elapsed_time(e1) * 1e3 / trial_steps
+                best = us if best is None else min(best, us)
+            timings[c] = best
             if verbose:
                 print(f"autotune {c}: {timings[c]:.2f} us/step")
     finally:
