@@ -149,7 +149,8 @@ def run_batched(steps: int, reps: int, dev):
                         "10x10 point stimulus, start U[0,5000], period U[15000,40000] steps"}
 
 
-def run_adjoint(dev, n_tissues: int = 16, steps: int = 5000, n_obs: int = 20, size: int = 256):
+def run_adjoint(dev, n_tissues: int = 16, steps: int = 5000, n_obs: int = 20, size: int = 256,
+                seg: int = None):
     """Gradient throughput of the inverse problem: a batch of 16 experiments on one 256x256
     scar-D tissue (parameter set 3), each with its own 10x10 point stimulus; observations of u
     at 20 evenly spaced checkpoints over 5000 steps; MSE loss against observations made with the
@@ -184,7 +185,7 @@ def run_adjoint(dev, n_tissues: int = 16, steps: int = 5000, n_obs: int = 20, si
         theta.grad = None
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        out = rollout_batch(s0, D, theta, stims, 0, steps, obs_t)
+        out = rollout_batch(s0, D, theta, stims, 0, steps, obs_t, seg=seg)
         loss = ((out[:, :, 2] - obs) ** 2).mean()
         loss.backward()
         torch.cuda.synchronize()
