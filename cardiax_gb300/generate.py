@@ -19,7 +19,10 @@ from typing import Sequence
 
 import torch
 
+import numpy as np
+
 from . import convert, io, scars
+from . import stimulus as S
 from .tissue import Tissue
 
 
@@ -64,3 +67,88 @@ def random_diffusivity(rng, shape: Sequence[int], domain: Sequence[float] = (0.0
     (deepx/generate.py:79-83): an (H, W) float32 device tensor."""
     c = scars.random_diffusivity_scar(rng, shape, device)
     return convert.diffusivity_rescale(c, domain)
+
+
+# ---- randomised experiments (deepx/generate.py:16-133) ---------------------------------------
+# The reference draws from JAX's PRNG; here every function takes a NumPy Generator (or a seed)
+# and draws the same distributions in the reference's order.
+
+def _rng(rng) -> np.random.Generator:
+    return rng if isinstance(rng, np.random.Generator) else np.random.default_rng(rng)
+
+
+def random_protocol(rng, min_start: int = 0, max_start: int = 1000, min_period: int = 400,
+                    max_period: int = int(1e9)) -> S.Protocol:
+    """Start in [min_start, max_start), duration 2 (instantaneous), period in
+    [min_period, max_period) (deepx/generate.py:16-27)."""
+    g = _rng(rng)
+    start = int(g.integers(int(min_start), int(max_start)))
+    period = int(g.integers(int(min_period), int(max_period)))
+    return S.Protocol(start, 2, period)
+
+
+def random_rectangular_stimulus(rng, shape, protocol: S.Protocol, modulus: float = 0.6,
+                                device=None) -> S.Stimulus:
+    """A rectangle of size in [max(H // 100, 10), H // 3) per side, centred in
+    [min(size), H) (deepx/generate.py:30-36)."""
+    g = _rng(rng)
+    size = g.integers(max(shape[0] // 100, 10), shape[0] // 3, size=2)
+    centre = g.integers(int(size.min()), shape[0], size=2)
+    return S.rectangular(shape, (int(centre[0]), int(centre[1])), (int(size[0]), int(size[1])),
+                         modulus, protocol, device=device)
+
+
+def random_linear_stimulus(rng, shape, protocol: S.Protocol, modulus: float = 0.6,
+                           device=None) -> S.Stimulus:
+    """A stripe of coverage 0.2 |N(0, 1)| along the north, east or south edge (the reference
+    draws the direction from [0, 3), so never west; deepx/generate.py:39-45)."""
+    g = _rng(rng)
+    coverage = abs(float(g.standard_normal()))
+    direction = S.Direction(int(g.integers(0, 3)))
+    return S.linear(shape, direction, coverage * 0.2, modulus, protocol, device=device)
+
+
+def random_triangular_stimulus(rng, shape, protocol: S.Protocol, modulus: float = 0.6,
+                               device=None) -> S.Stimulus:
+    """A stripe of coverage 0.2 |N(0, 1)| rotated by 45 |N(0, 1)| degrees
+    (deepx/generate.py:48-56)."""
+    g = _rng(rng)
+    angle, coverage = np.abs(g.standard_normal(2))
+    direction = S.Direction(int(g.integers(0, 3)))
+    return S.triangular(shape, direction, float(angle) * 45, float(coverage) * 0.2, modulus,
+                        protocol, device=device)
+
+
+def random_stimulus(rng, shape, min_start: int = 0, max_start: int = 0,
+                    device=None) -> S.Stimulus:
+    """A rectangular, triangular or linear stimulus of amplitude 20 with a random protocol
+    (deepx/generate.py:59-76; the reference's default max_start = 0 is an empty range, so callers
+    pass one)."""
+    g = _rng(rng)
+    protocol = random_protocol(g, min_start=min_start, max_start=max_start)
+    fns = (random_rectangular_stimulus, random_triangular_stimulus, random_linear_stimulus)
+    fn = fns[int(g.integers(0, len(fns)))]
+    return fn(g, shape, protocol=protocol, modulus=20.0, device=device)
+
+
+def random_sequence(rng, params, filepath: str = None, shape: Sequence[int] = (1200, 1200),
+                    n_stimuli: int = 2, start: float = 0, stop: float = 1000, step: float = 1,
+                    dt: float = 0.01, dx: float = 0.01, reshape: Sequence[int] = None,
+                    use_memory: bool = False, plot_while: bool = False, device=None):
+    """A random experiment (deepx/generate.py:86-133): ``n_stimuli`` stimuli whose starts are
+    spaced by ``tau_d`` seconds, a scar diffusivity map, and the sequence of states from
+    ``start`` to ``stop`` ms every ``step`` ms (:func:`sequence`).  Times in ms."""
+    g = _rng(rng)
+    shape = tuple(int(x) for x in shape)
+    starts = np.arange(1, convert.ms_to_units(stop, dt),
+                       convert.ms_to_units(params.tau_d * 1000, dt))
+    if len(starts) < n_stimuli:
+        raise ValueError("too few stimulus start slots before `stop`")
+    stimuli = [random_stimulus(g, shape, min_start=int(starts[i]), max_start=int(starts[i]) + 1,
+                               device=device) for i in range(n_stimuli)]
+    diffusivity = random_diffusivity(g, shape, device=device)
+    return sequence(start=convert.ms_to_units(start, dt), stop=convert.ms_to_units(stop, dt),
+                    step=convert.ms_to_units(step, dt), dt=dt, dx=dx, params=params,
+                    diffusivity=diffusivity, stimuli=stimuli, filename=filepath,
+                    reshape=reshape, use_memory=use_memory, plot_while=plot_while,
+                    device=device)

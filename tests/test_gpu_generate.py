@@ -118,3 +118,23 @@ def test_triangular_stimulus_matches_scipy(shape, angle):
         stripe = linear(shape, d, 0.2, 20.0, Protocol(0, 2, 1e9), device="cpu").field.numpy()
         ref = rotate(stripe, angle=angle, mode="nearest", prefilter=False, reshape=False)
         assert np.abs(got - ref).max() <= 1e-5, np.abs(got - ref).max()
+
+
+def test_random_sequence_end_to_end(tmp_path):
+    """deepx/generate.py:86-133 with NumPy draws: random stimuli (any of the three kinds), a scar
+    diffusivity map and the emitted sequence, written to the HDF5 data set."""
+    _gpu()
+    from cardiax_gb300 import generate, h5, params
+    path = str(tmp_path / "rand.hdf5")
+    states = generate.random_sequence(5, params.PARAMSET_3, path, shape=(64, 64), n_stimuli=1,
+                                      start=0, stop=2, step=0.5, reshape=(32, 32))
+    assert tuple(states.shape) == (4, 3, 32, 32)
+    assert torch.isfinite(states).all()
+    with h5.File(path) as f:
+        assert np.array_equal(f["states"][:], states.cpu().numpy())
+        D = f["diffusivity"][:]
+        assert D.shape == (32, 32) and 0.0001 - 1e-6 <= D.min() and D.max() <= 0.001 + 1e-6
+        assert f["start"][0] == 1 and f["duration"][0] == 2
+    for seed in range(3):
+        s = generate.random_triangular_stimulus(seed, (80, 80), generate.random_protocol(seed))
+        assert s.field.is_cuda and float(s.field.max()) <= 0.6 + 1e-6
