@@ -371,7 +371,12 @@ def run_next_rows(dev, reps: int = 2):
     * ``sequence``: deepx/generate.py:135-210 as the reference's data generation runs it --
       a 1200^2 tissue from rest, two triangular stimuli (modulus 20, 2 steps), 10 000 Euler
       steps, the state emitted every 100 steps resized to 256^2 on the device -- GCUPS of the
-      stepping with the emission included, and emitted states per second."""
+      stepping with the emission included, and emitted states per second;
+    * ``hdf5``: those 101 emitted states written as the reference's HDF5 data set
+      (cardiax/io.py:13-78; ``io.init`` + ``io.add_states``) from host memory, MB/s;
+    * ``scar``: deepx/utils_scars.py:409-426 at its default 1200^2 -- ms per scar map end to end
+      (host outlines, fill and blur kernels), and the blur kernel alone (K = 120 taps per axis)
+      in TFLOP/s."""
     import torch
     from cardiax_gb300 import generate, params as Pm
     from cardiax_gb300.stimulus import Direction, Protocol, Stimulus, triangular
@@ -407,14 +412,50 @@ def run_next_rows(dev, reps: int = 2):
              triangular((S, S), Direction.SOUTH, -45.0, 0.2, 20.0, Protocol(3000, 2, 1e9),
                         device=dev)]
 
+    emitted = {}
+
     def seq():
-        generate.sequence(0, n_steps + every, every, 0.01, 0.01, Pm.PARAMSET_3, Ds, stims,
-                          reshape=out, device=dev)
+        emitted["states"] = generate.sequence(0, n_steps + every, every, 0.01, 0.01,
+                                              Pm.PARAMSET_3, Ds, stims, reshape=out, device=dev)
     t_s = best(seq)
     seq_r = {"grid": f"{S}x{S}", "euler_steps": n_steps, "emit_every": every,
              "reshape": f"{out[0]}x{out[1]}", "gcups": S * S * n_steps / t_s / 1e9,
              "states_per_s": (n_steps // every) / t_s}
-    return {"heun": heun_r, "sequence": seq_r}
+
+    from cardiax_gb300 import io, scars
+    host = emitted["states"].cpu().numpy()
+    with tempfile.TemporaryDirectory() as tdir:
+        path = os.path.join(tdir, "sequence.hdf5")
+
+        def write():
+            f = io.init(path, out, n_iter=host.shape[0], n_stimuli=0)
+            io.add_states(f["states"], host, 0, host.shape[0])
+            f.close()
+        t_w = best(write)
+        file_bytes = os.path.getsize(path)
+    h5_r = {"states": int(host.shape[0]), "bytes": int(host.nbytes), "file_bytes": file_bytes,
+            "mb_per_s": host.nbytes / t_w / 1e6}
+
+    Hs = 1200
+    d = scars.draw(np.random.default_rng(7))
+    t_sc = best(lambda: scars.random_diffusivity_scar(d, (Hs, Hs), device=dev))
+    rows, cols = scars.outlines(d, (Hs, Hs))
+    K, sigma = scars.blur_width(d, (Hs, Hs))
+    wts = scars.gaussian_weights(K, sigma)
+    mask, _ = scars.rasterize(rows, cols, (Hs, Hs), dev)
+    scars.blur_same(mask, wts, one_minus=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(5):
+        scars.blur_same(mask, wts, one_minus=True)
+    e1.record()
+    torch.cuda.synchronize()
+    t_blur = e0.elapsed_time(e1) / 5 / 1e3
+    scar_r = {"size": f"{Hs}x{Hs}", "blobs": d.n_blobs, "taps": K,
+              "ms_per_map": t_sc * 1e3, "blur_ms": t_blur * 1e3,
+              "blur_tflops": 2.0 * K * K * Hs * Hs / t_blur / 1e12}
+    return {"heun": heun_r, "sequence": seq_r, "hdf5": h5_r, "scar": scar_r}
 
 
 def run_schedules(dev, sizes=(256, 512, 1024, 2048), steps: int = 400):

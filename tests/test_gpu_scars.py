@@ -57,9 +57,12 @@ def test_scar_field_matches_reference(golden):
         assert np.abs(got - field).max() <= _tol(K, w, np.ones(1)), shape
 
 
-@pytest.mark.parametrize("H,W", [(17, 23), (64, 64), (40, 100), (3, 5)])
-@pytest.mark.parametrize("K", [1, 2, 5, 8, 25, 41])
+@pytest.mark.parametrize("H,W,K", [(H, W, K) for H, W in [(17, 23), (64, 64), (40, 100), (3, 5),
+                                                          (130, 70)]
+                                   for K in [1, 2, 5, 8, 25, 41]]
+                         + [(20, 30, 520), (70, 66, 512)])
 def test_conv2d_same_matches_scipy(H, W, K):
+    """The tiled kernel (K <= 512) and the per-output fallback (K > 512)."""
     _gpu()
     from cardiax_gb300 import scars as P
     rng = np.random.default_rng(H * 1000 + W * 10 + K)
