@@ -294,3 +294,32 @@ def test_io_load_slices_every_root_dataset(tmp_path):
     assert len(got) == 2  # states, stimuli (name order)
     np.testing.assert_array_equal(got[0], x[1:6:2])
     assert got[1].shape == (0, 4, 5)
+
+
+def test_random_trees_round_trip(tmp_path):
+    """Seeded random trees of groups and datasets (names, dtypes, shapes, nesting) read back
+    exactly, and every file passes the structure walk."""
+    rng = np.random.default_rng(2024)
+    dtypes = [np.float32, np.float64, np.int64, np.int32, np.int16, np.uint8, np.uint32]
+    for case in range(12):
+        p = tmp_path / f"r{case}.h5"
+        want = {}
+        with h5.File(p, "w") as f:
+            for k in range(int(rng.integers(1, 40))):
+                depth = int(rng.integers(0, 3))
+                parts = [f"g{int(rng.integers(0, 4))}" for _ in range(depth)]
+                name = "/".join(parts + [f"d{k}_{'z' * int(rng.integers(0, 9))}"])
+                if any(name.startswith(w + "/") or w.startswith(name + "/") for w in want):
+                    continue
+                dt = dtypes[int(rng.integers(0, len(dtypes)))]
+                shape = tuple(int(x) for x in rng.integers(0, 6, size=int(rng.integers(0, 4))))
+                v = (rng.standard_normal(shape) * 100).astype(dt)
+                f.create_dataset(name, data=v)
+                want[name] = v
+        raw = _raw(p)
+        _, root, _, _, bt, hp = struct.unpack_from("<QQIIQQ", raw, 56)
+        _walk_group(raw, root, cached=(bt, hp))
+        with h5.File(p) as f:
+            for name, v in want.items():
+                got = f[name][()]
+                assert np.asarray(got).dtype == v.dtype and np.array_equal(got, v), name
