@@ -318,7 +318,12 @@ def test_random_trees_round_trip(tmp_path):
                 want[name] = v
         raw = _raw(p)
         _, root, _, _, bt, hp = struct.unpack_from("<QQIIQQ", raw, 56)
-        _walk_group(raw, root, cached=(bt, hp))
+        todo = [(root, (bt, hp))]
+        while todo:  # every group of the tree, its cached B-tree and heap checked
+            hdr, cached = todo.pop()
+            for _, (child, cache, scratch) in _walk_group(raw, hdr, cached=cached).items():
+                if cache == 1:
+                    todo.append((child, scratch))
         with h5.File(p) as f:
             for name, v in want.items():
                 got = f[name][()]
