@@ -11,8 +11,6 @@ import numpy as np
 import pytest
 import torch
 
-import fk_oracle as O
-
 pytestmark = pytest.mark.gpu
 
 P3 = (3.33, 19.6, 1250, 870, 41, 0.25, 12.5, 33.33, 29, 10, 0.85, 0.13, 0.04, 1)
