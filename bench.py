@@ -16,9 +16,13 @@ amplitude 20, Protocol(start=0, duration=200, period=20000) in steps), advanced 
                    per cell-update (read u, v, w, D; write u, v, w).
 * ``cpu_baseline`` the C restatement of the reference's stepper (the oracle port) on the host's
                    cores, on a bounded sample of the same workload.
-* ``schedules``    the roofline workload at 1024^2 and 2048^2 (a few hundred steps each) under
-                   every schedule: one launch per step (k = 1), temporal blocking with k = 2, 4,
-                   8 steps per launch, and the dataflow launch; all give identical bits.
+* ``schedules``    the roofline workload at 256^2, 512^2, 1024^2 and 2048^2 (a few hundred
+                   steps each) under every schedule: one launch per step (k = 1), temporal
+                   blocking with k = 2, 4, 8 steps per launch, the dataflow launch, and "auto"
+                   (the tissue autotuner's choice); all give identical bits.
+* ``batched``      256 mixed tissues in one launch per step vs a loop of per-tissue calls.
+* ``adjoint``      gradient throughput of the 16-experiment inverse problem (dL/dD, dL/dtheta).
+* ``next_rows``    Heun, the data-generation caller, the HDF5 write, the scar generator.
 
 ``--impl reference`` times that CPU implementation alone on the same workload (the reference's
 own JAX CPU path cannot be installed here; the port is its restatement).  Multi-GPU runs are
