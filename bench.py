@@ -16,12 +16,22 @@ amplitude 20, Protocol(start=0, duration=200, period=20000) in steps), advanced 
                    per cell-update (read u, v, w, D; write u, v, w).
 * ``cpu_baseline`` the C restatement of the reference's stepper (the oracle port) on the host's
                    cores, on a bounded sample of the same workload.
+* ``headline``     the figures below in one short block: plain stepper at 2048^2 and 4096^2,
+                   batched, adjoint and inverse problem.
+* ``parity``       max|du| of the GPU against the reference's own float32 run (every
+                   checkpoint) and its x64 run (1000 steps) on the 128^2 configuration, and
+                   against the float32 and float64 oracle on the CPU-baseline sample of the
+                   2048^2 workload, with the float32-vs-float64 gap beside each.
+* ``roofline_4096`` the same workload at 4096^2 (DRAM-bound: nothing stays in L2).
+* ``batched``      256 mixed tissues in one launch per step vs a loop of per-tissue calls,
+                   10^4 steps each.
+* ``adjoint``      gradient throughput of the 16-experiment inverse problem (dL/dD, dL/dtheta)
+                   against 116 algorithmic bytes per experiment cell and gradient step, and
+                   ``inverse``: 200 Adam iterations on D with the loss curve.
 * ``schedules``    the roofline workload at 256^2, 512^2, 1024^2 and 2048^2 (a few hundred
                    steps each) under every schedule: one launch per step (k = 1), temporal
                    blocking with k = 2, 4, 8 steps per launch, the dataflow launch, and "auto"
                    (the tissue autotuner's choice); all give identical bits.
-* ``batched``      256 mixed tissues in one launch per step vs a loop of per-tissue calls.
-* ``adjoint``      gradient throughput of the 16-experiment inverse problem (dL/dD, dL/dtheta).
 * ``next_rows``    Heun, the data-generation caller, the HDF5 write, the scar generator.
 
 ``--impl reference`` times that CPU implementation alone on the same workload (the reference's
@@ -46,6 +56,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 BYTES_PER_UPDATE = 28  # read u, v, w, D + write u, v, w (float32)
+# one gradient step of one experiment cell (float32): the forward step (28), its recomputation
+# (28) and the store of the recomputed state into the segment buffer (12), and the adjoint step
+# (read x_t 12, D 4, lambda_{t+1} 12; write lambda_t 12; read and write dL/dD 8 = 48)
+ADJ_BYTES_PER_GRAD_STEP = 28 + 28 + 12 + 48
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -134,19 +148,23 @@ def run_batched(steps: int, reps: int, dev):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / 1e3
 
-    timed(lambda: batch.advance(0, steps))  # warm-up
+    warm = max(2 * tune["graph_steps"], 64)
+    timed(lambda: batch.advance(0, warm))  # warm-up (graph capture)
     tb = min(timed(lambda: batch.advance(0, steps)) for _ in range(reps))
 
-    def loop():
+    def loop(n):
         for t in tissues:
-            t.advance(0, steps)
+            t.advance(0, n)
 
-    timed(loop)
-    tl = min(timed(loop) for _ in range(reps))
+    timed(lambda: loop(64))  # warm-up
+    tl = timed(lambda: loop(steps))  # one run: 256 x 1e4 launches
     batch.close()
+    peak, _ = peaks()
+    gcups = cells * steps / tb / 1e9
     return {"tissues": len(tissues), "cells": cells, "euler_steps": steps,
-            "gcups": cells * steps / tb / 1e9, "plain_loop_gcups": cells * steps / tl / 1e9,
-            "speedup_vs_plain_loop": tl / tb, "graph_steps": tune["graph_steps"],
+            "gcups": gcups, "plain_loop_gcups": cells * steps / tl / 1e9,
+            "speedup_vs_plain_loop": tl / tb, "frac": gcups * BYTES_PER_UPDATE / peak,
+            "graph_steps": tune["graph_steps"],
             "autotune_ms_per_step": {str(k): v for k, v in tune["ms_per_step"].items()},
             "workload": "256 tissues, sizes {64^2,128^2,256^2,512^2,256x1024}, sets "
                         "{1A,3,4A,5}, scar D (factor U[0,0.1], floor 1e-4, blur 2), plane or "
@@ -155,33 +173,18 @@ def run_batched(steps: int, reps: int, dev):
 
 def run_adjoint(dev, n_tissues: int = 16, steps: int = 5000, n_obs: int = 20, size: int = 256,
                 seg: int = None):
-    """Gradient throughput of the inverse problem: a batch of 16 experiments on one 256x256
-    scar-D tissue (parameter set 3), each with its own 10x10 point stimulus; observations of u
-    at 20 evenly spaced checkpoints over 5000 steps; MSE loss against observations made with the
-    true D; gradient w.r.t. D (65,536 values, shared by the batch) and the 13 parameters through
-    the adjoint kernel with sqrt(T) checkpointing (forward, segment recomputation and adjoint
-    each one launch per step for all 16 experiments).
+    """Gradient throughput of the inverse problem (``inverse_problem``: 16 experiments on one
+    256x256 scar-D tissue, u observed at 20 checkpoints over 5000 steps): MSE loss against the
+    observations made with the true D, gradient w.r.t. D (65,536 values, shared by the batch)
+    and the 13 parameters through the adjoint kernel with sqrt(T) checkpointing (forward,
+    segment recomputation and adjoint each one launch per step for all 16 experiments).
     ``grad_steps_per_s`` = experiments x steps / seconds of forward + backward."""
     import torch
-    from cardiax_gb300 import params as Pm
     from cardiax_gb300.adjoint import rollout_batch
-    from cardiax_gb300.stimulus import Protocol, Stimulus
 
-    rng = np.random.default_rng(4)
+    s0, D_true, theta0, stims, obs_t, obs = inverse_problem(dev, n_tissues, steps, n_obs, size)
     H = W = size
-    obs_t = [steps * (k + 1) // n_obs for k in range(n_obs)]
-    theta = torch.tensor(Pm.PARAMSET_3[:13], dtype=torch.float32, device=dev, requires_grad=True)
-    stims = []
-    for _ in range(n_tissues):
-        f = np.zeros((H, W), np.float32)
-        r, c = int(rng.integers(0, H - 10)), int(rng.integers(0, W - 10))
-        f[r:r + 10, c:c + 10] = 20.0
-        stims.append([Stimulus(Protocol(int(rng.integers(0, 500)), 200, 20000), f)])
-    s0 = torch.zeros((n_tissues, 3, H, W), device=dev)
-    s0[:, :2] = 1.0
-    D_true = torch.as_tensor(scar_diffusivity(rng, H, W), device=dev)
-    with torch.no_grad():
-        obs = rollout_batch(s0, D_true, theta.detach(), stims, 0, steps, obs_t)[:, :, 2]
+    theta = theta0.clone().requires_grad_(True)
     D = torch.full((H, W), 1e-3, device=dev, requires_grad=True)
     times = []
     for _ in range(2):
@@ -195,13 +198,172 @@ def run_adjoint(dev, n_tissues: int = 16, steps: int = 5000, n_obs: int = 20, si
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
     t_best = min(times)
+    peak, _ = peaks()
+    gbs = n_tissues * steps * H * W * ADJ_BYTES_PER_GRAD_STEP / t_best / 1e9
     return {"experiments": n_tissues, "size": f"{H}x{W}", "euler_steps": steps,
             "observations": n_obs, "seconds_per_gradient": t_best,
             "grad_steps_per_s": n_tissues * steps / t_best,
+            "algorithmic_bytes_per_grad_cell_step": ADJ_BYTES_PER_GRAD_STEP,
+            "achieved_gbs": gbs, "frac": gbs / peak,
             "gradient": "dL/dD (per cell, shared D) and dL/dtheta (13 parameters), MSE on u at "
                         "the observations, hand-written adjoint with sqrt(T) checkpoint-recompute",
             "checked": "relative error <= 1e-3 vs float64 autodiff of the oracle and central "
                        "finite differences (tests/test_gpu_adjoint.py)"}
+
+
+def inverse_problem(dev, n_tissues: int = 16, steps: int = 5000, n_obs: int = 20,
+                    size: int = 256, seed: int = 4):
+    """The inverse problem's data: 16 experiments on one 256x256 scar-D tissue (parameter set
+    3), each with its own 10x10 point stimulus (amplitude 20, start in [0, 500) steps); u
+    observed at 20 evenly spaced checkpoints over 5000 steps with the true D.  Returns
+    (states0, D_true, theta, stimuli, obs_times, observations)."""
+    import torch
+    from cardiax_gb300 import params as Pm
+    from cardiax_gb300.adjoint import rollout_batch
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+
+    rng = np.random.default_rng(seed)
+    H = W = size
+    obs_t = [steps * (k + 1) // n_obs for k in range(n_obs)]
+    theta = torch.tensor(Pm.PARAMSET_3[:13], dtype=torch.float32, device=dev)
+    stims = []
+    for _ in range(n_tissues):
+        f = np.zeros((H, W), np.float32)
+        r, c = int(rng.integers(0, H - 10)), int(rng.integers(0, W - 10))
+        f[r:r + 10, c:c + 10] = 20.0
+        stims.append([Stimulus(Protocol(int(rng.integers(0, 500)), 200, 20000), f)])
+    s0 = torch.zeros((n_tissues, 3, H, W), device=dev)
+    s0[:, :2] = 1.0
+    D_true = torch.as_tensor(scar_diffusivity(rng, H, W), device=dev)
+    with torch.no_grad():
+        obs = rollout_batch(s0, D_true, theta, stims, 0, steps, obs_t)[:, :, 2]
+    return s0, D_true, theta, stims, obs_t, obs
+
+
+def run_inverse(dev, iterations: int = 200, lr: float = 2e-5):
+    """The inverse problem end to end: Adam on D (65,536 values) from a uniform D = 0.001,
+    ``iterations`` gradient evaluations of the 16 x 5000-step rollout (adjoint.fit_diffusivity),
+    D clipped to [1e-4, 2e-3] after each step."""
+    import torch
+    from cardiax_gb300.adjoint import fit_diffusivity
+
+    s0, D_true, theta, stims, obs_t, obs = inverse_problem(dev)
+    D0 = torch.full_like(D_true, 1e-3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    D, losses = fit_diffusivity(s0, D0, theta, stims, 0, obs_t[-1], obs_t, obs,
+                                iterations=iterations, lr=lr)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    rel = lambda X: float((X - D_true).norm() / D_true.norm())  # noqa: E731
+    drops = sum(1 for a, b in zip(losses, losses[1:]) if b < a)
+    return {"iterations": iterations, "optimizer": f"Adam(lr={lr:g}) on D, clip [1e-4, 2e-3]",
+            "seconds_per_iteration": dt / max(1, iterations),
+            "loss_first": losses[0] if losses else None,
+            "loss_last": losses[-1] if losses else None,
+            "loss_min": min(losses) if losses else None,
+            "loss_decreasing_steps": f"{drops}/{max(0, len(losses) - 1)}",
+            "loss_every_20": losses[::20],
+            "D_rel_error_first": rel(D0), "D_rel_error_last": rel(D)}
+
+
+def run_roofline_sample(dev, size: int = 4096, steps: int = 300):
+    """The roofline workload at ``size`` (4096^2: the state, D and the new state do not fit in
+    L2, so the step is DRAM-bound): best of 2 runs of ``steps`` steps, L2 flushed before each."""
+    import torch
+    from cardiax_gb300 import params
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    from cardiax_gb300.tissue import Tissue
+
+    D, field, proto = workload(size, size)
+    tis = Tissue((size, size), params.PARAMSET_3, D, [Stimulus(Protocol(*proto), field)],
+                 device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    tis.advance(0, 8)
+    best = None
+    for rep in range(2):
+        tis.init()
+        flush.fill_(float(rep))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        tis.advance(0, steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del flush
+    us = best * 1e3 / steps
+    peak, _ = peaks()
+    gbs = BYTES_PER_UPDATE * size * size / (us * 1e-6) / 1e9
+    return {"size": f"{size}x{size}", "steps": steps, "us_per_step": us,
+            "gcups": size * size / (us * 1e-6) / 1e9, "achieved_gbs": gbs, "frac": gbs / peak,
+            "traffic": profiled_traffic(f"fk_step_kernel_{size}.md"),
+            "traffic_source": f"profiles/fk_step_kernel_{size}.md (ncu, one launch)"}
+
+
+def run_parity_config1(dev):
+    """The 128x128 configuration, 1000 steps, checkpoints every 100 (plain: amplitude 1 for the
+    2 active steps, no wave; excite: amplitude 20, a travelling wave) against the reference's
+    own float32 run at every checkpoint and its x64 run at 1000 steps (tests/golden fixtures
+    made by running the reference's solve.py)."""
+    from cardiax_gb300 import params, solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+
+    gdir = os.path.join(ROOT, "tests", "golden")
+    g32 = np.load(os.path.join(gdir, "config0.npz"))
+    g64 = np.load(os.path.join(gdir, "config0_x64.npz"))
+    out = {}
+    for tag, proto in (("plain", (0, 200, 1e9)), ("excite", (0, 2, 1e9))):
+        D = np.full((128, 128), 0.001, np.float32)
+        states = solve.forward(solve.init((128, 128), device=dev), list(range(0, 1001, 100)),
+                               params.PARAMSET_3, D,
+                               [Stimulus(Protocol(*proto), g32[f"{tag}_field"])], 0.01, 0.01)
+        e32 = max(float(np.abs(s.u.cpu().numpy() - g32[f"{tag}_u_{(i + 1) * 100}"]).max())
+                  for i, s in enumerate(states))
+        u = states[-1].u.cpu().numpy().astype(np.float64)
+        out[tag] = {"max_du_vs_ref_f32": e32,
+                    "du_vs_ref_x64_1000": float(np.abs(u - g64[f"{tag}_u_1000"]).max()),
+                    "ref_f32_vs_x64_1000": float(np.abs(g32[f"{tag}_u_1000"] -
+                                                        g64[f"{tag}_u_1000"]).max())}
+    return out
+
+
+def cpu_baseline_leg(tis, H, W, D, field, proto, seconds: float, threads: int):
+    """The CPU baseline: the C oracle (float32, ``threads`` host threads) timed on a bounded
+    sample of the workload (the first n steps from rest, n chosen for about ``seconds``); then,
+    as the checker, the same sample in float64, and the GPU's state after the same n steps
+    compared with both."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fk_oracle as O
+    import fk_oracle_c as C
+    C.build()
+    from cardiax_gb300 import params
+    P3 = params.PARAMSET_3
+    stims = [(proto[0], proto[1], proto[2], field)]
+    st = O.init((H, W))
+    t0 = time.perf_counter()
+    C.forward_euler(st, 0, 2, P3, D, stims, 0.01, 0.01, threads=threads)
+    per = max((time.perf_counter() - t0) / 2, 1e-4)
+    n = int(max(2, min(2000, seconds / per)))
+    t0 = time.perf_counter()
+    v, w, u = C.forward_euler(st, 0, n, P3, D, stims, 0.01, 0.01, threads=threads)
+    dt = time.perf_counter() - t0
+    rate = H * W * n / dt / 1e9
+    cpu = {"value": rate, "unit": "GCUPS", "cores": threads, "kind": "port",
+           "sample": f"{H}x{W}, the first {n} Euler steps from rest ({dt:.1f} s), C "
+                     f"restatement of cardiax/solve.py with OpenMP over rows"}
+    st64 = O.init((H, W), np.float64)
+    stims64 = [(proto[0], proto[1], proto[2], field.astype(np.float64))]
+    _, _, u64 = C.forward_euler(st64, 0, n, P3, D.astype(np.float64), stims64, 0.01, 0.01,
+                                threads=threads)
+    tis.init()
+    tis.advance(0, n)
+    ug = tis.view()[2].cpu().numpy()
+    parity = {"size": f"{H}x{W}", "steps": n,
+              "max_du_vs_oracle_f32": float(np.abs(ug - u).max()),
+              "max_du_vs_oracle_f64": float(np.abs(ug.astype(np.float64) - u64).max()),
+              "oracle_f32_vs_f64": float(np.abs(u.astype(np.float64) - u64).max())}
+    return cpu, parity
 
 
 def workload(H: int, W: int, seed: int = 1234):
@@ -599,36 +761,49 @@ def run_ours(args):
                 "algorithmic_bytes_per_launch": BYTES_PER_UPDATE * H * W,
                 "avg_launch_us": launch_ms * 1e3}
 
-    batched = None
-    if not args.no_batched:
-        batched = run_batched(args.batched_steps, 2, dev)
-    adjoint = None
-    if not args.no_adjoint:
-        adjoint = run_adjoint(dev)
-    schedules = None
-    if not args.no_schedules:
-        schedules = run_schedules(dev)
-    next_rows = None
-    if not args.no_next:
-        next_rows = run_next_rows(dev)
-
+    # sub-benchmarks (rank 0 of a replica run only: they are per-GPU figures)
+    solo = rank == 0
+    sample = run_roofline_sample(dev) if solo and not args.no_4096 else None
+    parity = None
+    if solo and not args.no_parity:
+        parity = {"config1_128x128_1000_steps": run_parity_config1(dev)}
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        r, n, dt = cpu_port_rate(H, W, D, field, proto, args.cpu_seconds, threads)
-        cpu = {"value": r, "unit": "GCUPS", "cores": threads, "kind": "port",
-               "sample": f"{H}x{W}, {n} Euler steps ({dt:.1f} s), C restatement of "
-                         f"cardiax/solve.py with OpenMP over rows"}
+    if solo and world == 1 and not args.no_cpu:
+        cpu, parity_2048 = cpu_baseline_leg(tis, H, W, D, field, proto, args.cpu_seconds,
+                                            os.cpu_count() or 1)
+        if parity is not None:
+            parity[f"roofline_{H}_sample"] = parity_2048
+    batched = run_batched(args.batched_steps, 2, dev) if solo and not args.no_batched else None
+    adjoint = None
+    if solo and not args.no_adjoint:
+        adjoint = run_adjoint(dev)
+        if args.inverse_iterations > 0:
+            adjoint["inverse"] = run_inverse(dev, iterations=args.inverse_iterations)
+    schedules = run_schedules(dev) if solo and not args.no_schedules else None
+    next_rows = run_next_rows(dev) if solo and not args.no_next else None
 
     if rank == 0:
+        def pick(d, *keys):
+            return None if d is None else {k: d.get(k) for k in keys}
+        headline = {
+            f"plain_{H}": {"gcups": value / world, "frac": roofline["frac"]},
+            "plain_4096": pick(sample, "gcups", "frac", "us_per_step"),
+            "batched": pick(batched, "gcups", "frac", "plain_loop_gcups",
+                            "speedup_vs_plain_loop", "euler_steps"),
+            "adjoint": pick(adjoint, "grad_steps_per_s", "seconds_per_gradient", "frac"),
+            "inverse": pick((adjoint or {}).get("inverse"), "iterations",
+                            "seconds_per_iteration", "loss_first", "loss_last",
+                            "D_rel_error_first", "D_rel_error_last"),
+        }
         out = {"metric": METRIC, "value": value, "unit": "GCUPS", "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup,
                "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-               "config": config(args), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-               "gpu_launches": args.steps * (S + 1), "clocks": clk, "batched": batched,
-               "adjoint": adjoint, "schedules": schedules, "next_rows": next_rows,
-               "wall_s_timed_region": t_wall}
+               "config": config(args), "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu,
+               "gpu_launches": args.steps * (S + 1), "clocks": clk,
+               "headline": headline, "parity": parity, "roofline_4096": sample,
+               "batched": batched, "adjoint": adjoint, "wall_s_timed_region": t_wall,
+               "schedules": schedules, "next_rows": next_rows}
         print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()
@@ -651,7 +826,11 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-schedules", action="store_true")
     ap.add_argument("--no-next", action="store_true", help="skip the Heun and sequence timings")
-    ap.add_argument("--batched-steps", type=int, default=2000)
+    ap.add_argument("--batched-steps", type=int, default=10000)
+    ap.add_argument("--inverse-iterations", type=int, default=200,
+                    help="Adam iterations of the inverse problem (0: skip)")
+    ap.add_argument("--no-4096", action="store_true", help="skip the 4096^2 roofline sample")
+    ap.add_argument("--no-parity", action="store_true", help="skip the parity figures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

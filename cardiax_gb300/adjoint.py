@@ -368,3 +368,36 @@ def rollout_batch(states0, D, theta, stimuli_per_tissue, t0: int, t1: int,
     (B, n_obs, 3, H, W); gradients flow to states0, D (summed over tissues) and theta."""
     return _RolloutBatch.apply(states0, D, theta, Cm, [list(s) for s in stimuli_per_tissue],
                                int(t0), int(t1), list(obs_times), float(dt), float(dx), seg)
+
+
+def fit_diffusivity(states0, D_init, theta, stimuli_per_tissue, t0: int, t1: int,
+                    obs_times: Sequence[int], observations, iterations: int = 200,
+                    lr: float = 2e-5, bounds=(1e-4, 2e-3), dt: float = 0.01, dx: float = 0.01,
+                    Cm: float = 1.0, seg: int = None, callback=None):
+    """The inverse problem: fits the per-cell diffusivity map to recordings of u.
+
+    ``observations`` is (B, n_obs, H, W): u of B experiments (sharing D and the parameters
+    ``theta``, each with its own initial state in ``states0`` (B, 3, H, W) and stimulus list)
+    at ``obs_times``.  Each iteration runs :func:`rollout_batch` (forward, then the adjoint
+    with sqrt(T) checkpoint-recompute), takes the mean squared error of u against the
+    observations, and makes one Adam step on D (learning rate ``lr``, in the units of D),
+    after which D is clipped to ``bounds`` (the explicit scheme needs D >= 0 and small enough
+    for stability).  ``callback(it, loss, D)`` is called after every step.  Returns the fitted
+    D and the list of losses (the loss of each iteration's D, before its step)."""
+    D = D_init.detach().clone().to(torch.float32).requires_grad_(True)
+    theta = theta.detach()
+    opt = torch.optim.Adam([D], lr=lr)
+    losses = []
+    for it in range(int(iterations)):
+        opt.zero_grad(set_to_none=True)
+        out = rollout_batch(states0, D, theta, stimuli_per_tissue, t0, t1, obs_times, dt, dx,
+                            Cm, seg)
+        loss = ((out[:, :, 2] - observations) ** 2).mean()
+        loss.backward()
+        opt.step()
+        with torch.no_grad():
+            D.clamp_(float(bounds[0]), float(bounds[1]))
+        losses.append(float(loss))
+        if callback is not None:
+            callback(it, losses[-1], D)
+    return D.detach(), losses

@@ -36,18 +36,62 @@ namespace fk {
 static __device__ int g_status_word;
 
 static std::mutex g_mu;
-static int *g_status_ptr[64];
+
+// ---- current context ------------------------------------------------------------------------
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext *);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long *);
+static PfnCtxGetCurrent g_ctx_get_current = nullptr;
+static PfnCtxGetId g_ctx_get_id = nullptr;
+static std::once_flag g_ctx_once;
+
+uint64_t context_id() {
+    std::call_once(g_ctx_once, [] {
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) ==
+                cudaSuccess && qa == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) ==
+                cudaSuccess && qb == cudaDriverEntryPointSuccess) {
+            g_ctx_get_current = reinterpret_cast<PfnCtxGetCurrent>(a);
+            g_ctx_get_id = reinterpret_cast<PfnCtxGetId>(b);
+        }
+    });
+    if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return (uint64_t)id;
+}
+
+bool context_changed(uint64_t &seen) {
+    const uint64_t now = context_id();
+    if (now != 0 && now == seen) return false;
+    seen = now;
+    return true;
+}
+
+// The device address of the error word in the current context (looked up again whenever the
+// context changes: a cudaDeviceReset invalidates the previous address).
+struct CtxAddr {
+    uint64_t ctx;
+    void *ptr;
+};
+static CtxAddr g_status_ptr[64];
 
 int *status_ptr() {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_status_ptr[dev]) {
+    CtxAddr &c = g_status_ptr[dev];
+    const uint64_t ctx = context_id();
+    if (!c.ptr || ctx == 0 || ctx != c.ctx) {
         void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_status_word) != cudaSuccess) return nullptr;
-        g_status_ptr[dev] = static_cast<int *>(p);
+        if (cudaGetSymbolAddress(&p, g_status_word) != cudaSuccess || !p) return nullptr;
+        c.ptr = p;
+        c.ctx = context_id();  // the lookup created the context if there was none
     }
-    return g_status_ptr[dev];
+    return static_cast<int *>(c.ptr);
 }
 
 // ---- TMA descriptors ---------------------------------------------------------------------

@@ -11,6 +11,13 @@
 namespace fk {
 
 int *status_ptr();
+// Unique id of the calling thread's current CUDA context (cuCtxGetId), 0 when there is none
+// yet or the driver cannot tell.  Ids are never reused within a process, so a cache of
+// per-context state (symbol addresses, function attributes) keyed on it is refreshed after a
+// cudaDeviceReset or any other context teardown.
+uint64_t context_id();
+// True, and `seen` updated, when the current context differs from `seen` (or is unknown).
+bool context_changed(uint64_t &seen);
 int make_plane_map(CUtensorMap *map, const float *plane, int64_t H, int64_t W, int64_t pitch,
                    int box_w, int box_h);
 int check_grid(const fk_grid &g);

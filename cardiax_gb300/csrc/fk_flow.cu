@@ -33,6 +33,7 @@
 // are resident (cooperative launch), and an item only waits on items with smaller numbers, which
 // every CTA processes in increasing order and publishes before it blocks, so no wait is
 // circular.
+#include "fk_capi_internal.h"
 #include "fk_tile.cuh"
 
 namespace fk {
@@ -300,28 +301,32 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
 }
 
 cudaError_t launch_flow(const FlowMaps &maps, const FlowArgs &a, bool act, cudaStream_t stream) {
-    static thread_local int configured_device = -1;
+    static thread_local uint64_t configured_ctx = 0;  // attributes belong to the context
     static thread_local int resident = 0;  // co-resident CTAs per device
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev != configured_device) {
+    if (context_changed(configured_ctx)) {
+        resident = 0;
         if ((e = cudaFuncSetAttribute(fk_flow_kernel<true>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       SMEM_FLOW_BYTES)) != cudaSuccess ||
             (e = cudaFuncSetAttribute(fk_flow_kernel<false>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      SMEM_FLOW_BYTES)) != cudaSuccess)
+                                      SMEM_FLOW_BYTES)) != cudaSuccess) {
+            configured_ctx = 0;
             return e;
+        }
         int per_sm_t = 0, per_sm_f = 0, sms = 0;
         if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_t, fk_flow_kernel<true>, NT,
                                                                SMEM_FLOW_BYTES)) != cudaSuccess ||
             (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_f, fk_flow_kernel<false>, NT,
                                                                SMEM_FLOW_BYTES)) != cudaSuccess ||
-            (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+            (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) {
+            configured_ctx = 0;
             return e;
+        }
         resident = (per_sm_t < per_sm_f ? per_sm_t : per_sm_f) * sms;
-        configured_device = dev;
     }
     if (resident < 1) return cudaErrorInvalidConfiguration;
     const int64_t ntiles = flow_flag_words(a.in[0].H, a.in[0].W) - 1;

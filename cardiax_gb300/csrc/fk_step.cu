@@ -4,6 +4,7 @@
 //
 // Replaces cardiax/solve.py:26-70 (step + step_euler, with gradient x6, stimulate and the edge
 // pads fused).
+#include "fk_capi_internal.h"
 #include "fk_tile.cuh"
 
 namespace fk {
@@ -221,20 +222,19 @@ __global__ void batch_copyback_kernel(const BatchTissue *tissues) {
 cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
                               const BatchItem *items, int n_items, const int *t_dev, int t_offset,
                               int parity, bool act, int *status, int grid, cudaStream_t stream) {
-    static thread_local int configured_device = -1;
-    int dev = -1;
-    cudaGetDevice(&dev);
-    if (dev != configured_device) {
+    // function attributes belong to the context: set again whenever it changes
+    static thread_local uint64_t configured_ctx = 0;
+    if (context_changed(configured_ctx)) {
         cudaError_t e;
         if ((e = cudaFuncSetAttribute(fk_batch_kernel<true>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      SMEM_BATCH_BYTES)) != cudaSuccess)
-            return e;
-        if ((e = cudaFuncSetAttribute(fk_batch_kernel<false>,
+                                      SMEM_BATCH_BYTES)) != cudaSuccess ||
+            (e = cudaFuncSetAttribute(fk_batch_kernel<false>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      SMEM_BATCH_BYTES)) != cudaSuccess)
+                                      SMEM_BATCH_BYTES)) != cudaSuccess) {
+            configured_ctx = 0;
             return e;
-        configured_device = dev;
+        }
     }
     if (grid > n_items) grid = n_items;
     if (grid < 1) return cudaSuccess;
@@ -290,22 +290,22 @@ bool l2_fits_step(int64_t H, int64_t pitch) {
 
 cudaError_t launch_step(const StepMaps &maps, const StepArgs &a, bool deriv, cudaStream_t stream,
                         int heun) {
-    // the attribute is per function and per device; setting it is cheap and idempotent
-    static thread_local int configured_device = -1;
-    int dev = -1;
-    cudaGetDevice(&dev);
-    if (dev != configured_device) {
-        cudaError_t e;
-        if ((e = set_smem_attr<true, false>()) != cudaSuccess) return e;
-        if ((e = set_smem_attr<false, true>()) != cudaSuccess) return e;
-        if ((e = set_smem_attr<false, false>()) != cudaSuccess) return e;
-        if ((e = set_smem_attr<false, false, 1>()) != cudaSuccess) return e;
-        if ((e = set_smem_attr<false, false, 2>()) != cudaSuccess) return e;
-        configured_device = dev;
-    }
+    // the attribute is per function and per context: set again whenever the context changes
+    static thread_local uint64_t configured_ctx = 0;
     static thread_local int n_sm = 0;
-    if (n_sm == 0 && cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-        return cudaErrorInvalidValue;
+    if (context_changed(configured_ctx)) {
+        cudaError_t e;
+        int dev = -1;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess || (e = set_smem_attr<true, false>()) != cudaSuccess ||
+            (e = set_smem_attr<false, true>()) != cudaSuccess ||
+            (e = set_smem_attr<false, false>()) != cudaSuccess ||
+            (e = set_smem_attr<false, false, 1>()) != cudaSuccess ||
+            (e = set_smem_attr<false, false, 2>()) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) {
+            configured_ctx = 0;
+            return e;
+        }
+    }
     const int ntiles = ((a.W + TX - 1) / TX) * ((a.H + TY - 1) / TY);
     const int grid = ntiles < n_sm * CTAS_PER_SM ? ntiles : n_sm * CTAS_PER_SM;
     cudaLaunchConfig_t cfg = {};

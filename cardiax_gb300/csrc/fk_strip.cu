@@ -3,6 +3,7 @@
 //
 // Replaces cardiax/solve.py:26-70 (step + step_euler, with gradient x6, stimulate and the edge
 // pads fused), like fk_step_kernel, and produces the same bits.
+#include "fk_capi_internal.h"
 #include "fk_strip.cuh"
 #include "fk_tile.cuh"
 
@@ -321,23 +322,22 @@ __global__ void __launch_bounds__(S_NT, S_CTAS_PER_SM)
 }
 
 cudaError_t launch_strip(const StripMaps &maps, const StepArgs &a, cudaStream_t stream) {
-    static thread_local int configured_device = -1;
+    static thread_local uint64_t configured_ctx = 0;  // attributes belong to the context
     static thread_local int n_sm = 0;
-    int dev = -1;
-    cudaGetDevice(&dev);
-    if (dev != configured_device) {
+    if (context_changed(configured_ctx)) {
         cudaError_t e;
-        if ((e = cudaFuncSetAttribute(fk_strip_kernel<false>,
+        int dev = -1;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+            (e = cudaFuncSetAttribute(fk_strip_kernel<false>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      S_SMEM_BYTES)) != cudaSuccess)
-            return e;
-        if ((e = cudaFuncSetAttribute(fk_strip_kernel<true>,
+                                      S_SMEM_BYTES)) != cudaSuccess ||
+            (e = cudaFuncSetAttribute(fk_strip_kernel<true>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      S_SMEM_BYTES)) != cudaSuccess)
+                                      S_SMEM_BYTES)) != cudaSuccess ||
+            (e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) {
+            configured_ctx = 0;
             return e;
-        if ((e = cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
-            return e;
-        configured_device = dev;
+        }
     }
     const int ntiles = (int)(((a.W + S_TX - 1) / S_TX) * ((a.H + S_TY - 1) / S_TY));
     const int cap = n_sm * S_CTAS_PER_SM;

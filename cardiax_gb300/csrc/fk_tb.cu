@@ -19,6 +19,7 @@
 // Each blocked step recomputes the halo ring of the tile: the work per useful cell-update is
 // sum_s |R_s| / (K |tile|), 1.2 for K = 2 on 32 x 64, 1.7 for K = 4, 8.9 for K = 8 on 16 x 16
 // (the only K = 8 tile that fits in shared memory).
+#include "fk_capi_internal.h"
 #include "fk_tile.cuh"
 #include "fk_tb.cuh"
 
@@ -326,16 +327,17 @@ cudaError_t launch_tb_k(const TbMaps &maps, const StepArgs &a, int64_t t0, cudaS
     using G = TbGeom<K, OY, OX>;
     constexpr int SMEM = G::BYTES + 16 + SMEM_ARGS_BYTES + 128;
     static_assert(SMEM <= 227 * 1024, "blocked tile does not fit in shared memory");
-    static thread_local int configured_device = -1;
+    static thread_local uint64_t configured_ctx = 0;  // attributes belong to the context
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev != configured_device) {
+    if (context_changed(configured_ctx)) {
         if ((e = cudaFuncSetAttribute(fk_tb_kernel<K, OY, OX, NTH>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM)) !=
-            cudaSuccess)
+            cudaSuccess) {
+            configured_ctx = 0;
             return e;
-        configured_device = dev;
+        }
     }
     int sms = 0;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)

@@ -2,8 +2,10 @@
  * cardiax_gb300 -- C ABI of the GB300 Fenton-Karma stepper.
  *
  * Plain pointers and sizes only.  Every device pointer is a CUDA device address; `stream` is a
- * cudaStream_t (NULL = the legacy default stream).  No entry point allocates device memory:
- * callers pass every buffer, including the ping-pong scratch state.
+ * cudaStream_t (NULL = the legacy default stream).  No entry point allocates device memory.
+ * Callers pass every buffer, including the ping-pong scratch state -- except for
+ * fk_forward_euler_noalloc, whose scratch state is a fixed-size device array owned by the
+ * library (see its declaration for the limit and the sharing rules).
  *
  * Layout
  *   A grid is H rows x W columns of float32 with a row pitch of `pitch` elements
@@ -111,9 +113,12 @@ int fk_forward_euler(fk_grid g, float *state, float *scratch, const float *D, co
  * (an XLA custom call, for instance, gets all of its buffers from XLA and must not allocate).
  * No counterpart in the reference.  The scratch state is a file-scope device array of this
  * library holding FK_NOALLOC_MAX_CELLS cells (H * pitch <= 512 * 512, 3 MiB per GPU for the
- * life of the process); larger grids return FK_ERR_CAPACITY.  The first call on a device looks
- * up the array's address (make it before any stream capture); calls that overlap on the GPU
- * share the array and race; nothing needs clearing between calls. */
+ * life of the process); larger grids return FK_ERR_CAPACITY.  The first call on a device, and
+ * the first one after that device's context changed (a cudaDeviceReset, for instance), looks up
+ * the array's address: make it before any stream capture.  Calls that overlap on the GPU share
+ * the array and race.  Nothing needs clearing between calls: the in-grid cells of the result
+ * never depend on earlier calls, and the state's row padding (columns W .. pitch-1) comes back
+ * unchanged. */
 #define FK_NOALLOC_MAX_CELLS (512 * 512)
 int fk_forward_euler_noalloc(fk_grid g, float *state, const float *D, const fk_params *p,
                              const fk_stimulus *stimuli, int n_stimuli, int64_t t0, int64_t t1,

@@ -19,6 +19,16 @@ Fixtures (all float32 unless noted; "x64" = the same code with float64, JAX's x6
 * ``config0.npz``          -- ``solve.forward`` on the 128x128 plain configuration (planar
   stimulus on the left 5 columns, amplitude 1.0, Protocol(0, 200, 1e9), checkpoints every
   100 steps to 1000) and its excitable variant (amplitude 20, Protocol(0, 2, 1e9))
+* ``paramsets.npz``        -- ``solve.forward`` for 1000 steps (checkpoints every 250: float32
+  u at each, v, w, u of both precisions at the last) on a 48x60 grid with a smooth D map, a
+  planar (8 columns) and a point (8x8) stimulus, under parameter sets 1A, 4A and 5 (the batched workload's sets besides
+  3) and 2 (a set with MAXFLOAT entries), float32 and x64
+
+* ``config0_x64.npz``      -- the configuration-0 runs of ``config0.npz`` with x64 (float64): u
+  at 1000 steps, the error reference of the benchmark's parity figures
+
+``--only NAME`` regenerates one fixture group (e.g. ``--only paramsets``) and leaves the other
+files untouched.
 """
 from __future__ import annotations
 
@@ -50,12 +60,66 @@ def smooth_field(rng, shape, lo, hi, dtype=np.float32):
     return (lo + (hi - lo) * f).astype(dtype)
 
 
-def main(root: str):
+PARAMSET_CASES = ("1A", "4A", "5", "2")
+
+
+def paramset_fixtures(R, R64, out):
+    """``forward`` under parameter sets other than 3 (1000 steps, float32 and x64)."""
+    rng = np.random.default_rng(SEED + 1)
+    shp = (48, 60)
+    D = smooth_field(rng, shp, 3e-4, 1e-3)
+    # 8 columns: a narrower 2-step pulse does not start a wave under sets 1A, 4A, 5
+    f1 = np.zeros(shp, np.float32)
+    f1[:, :8] = 20.0
+    f2 = np.zeros(shp, np.float32)
+    f2[30:38, 40:48] = 20.0
+    ck = np.arange(0, 1001, 250)
+    ps = {"D": D, "f1": f1, "f2": f2, "checkpoints": ck}
+    for name in PARAMSET_CASES:
+        for R_, dt_ in ((R, np.float32), (R64, np.float64)):
+            P_ = getattr(R_.params, f"PARAMSET_{name}")
+            stims = [R_.stimulus.Stimulus(R_.stimulus.Protocol(0, 2, 1e9), f1.astype(dt_)),
+                     R_.stimulus.Stimulus(R_.stimulus.Protocol(300, 2, 1e9), f2.astype(dt_))]
+            states = R_.solve.forward(R_.solve.init(shp), ck, P_, D.astype(dt_), stims, 0.01,
+                                      0.01)
+            print()
+            tag = "f32" if dt_ == np.float32 else "f64"
+            # float32: u at every checkpoint; both: v, w, u at the last
+            for i, st in enumerate(states if tag == "f32" else states[-1:]):
+                ps[f"{name}_{tag}_u_{ck[i + 1] if tag == 'f32' else ck[-1]}"] = np.asarray(st.u)
+            ps[f"{name}_{tag}_v_{ck[-1]}"] = np.asarray(states[-1].v)
+            ps[f"{name}_{tag}_w_{ck[-1]}"] = np.asarray(states[-1].w)
+    np.savez_compressed(os.path.join(out, "paramsets.npz"), **ps)
+
+
+def config0_x64_fixtures(R64, out):
+    """The 128x128 configuration (plain and excitable) in float64, u at 1000 steps."""
+    shp = (128, 128)
+    D = np.full(shp, 0.001, np.float64)
+    ck = np.arange(0, 1001, 100)
+    c0 = {}
+    for tag, amp, proto in (("plain", 1.0, (0, 200, 1e9)), ("excite", 20.0, (0, 2, 1e9))):
+        stim = R64.stimulus.linear(shp, R64.stimulus.Direction.WEST, 5 / 128, amp,
+                                   R64.stimulus.Protocol(*proto))
+        states = R64.solve.forward(R64.solve.init(shp), ck, R64.params.PARAMSET_3, D, [stim],
+                                   0.01, 0.01)
+        print()
+        c0[f"{tag}_u_1000"] = np.asarray(states[-1].u, np.float64)
+    np.savez_compressed(os.path.join(out, "config0_x64.npz"), **c0)
+
+
+def main(root: str, only: str = None):
     R = load_reference(root=root)
     R64 = load_reference(x64=True, root=root)
     S, P = R.solve, R.params
     rng = np.random.default_rng(SEED)
     out = HERE
+    if only in ("paramsets", "config0_x64"):
+        (paramset_fixtures(R, R64, out) if only == "paramsets" else config0_x64_fixtures(R64, out))
+        print("fixtures written to", out)
+        return
+    if only is not None:
+        raise SystemExit(f"unknown fixture group {only!r}")
 
     # --- stimulus schedule (tests/macro/stimulate_test.py:8-18, current stimulate) ---------
     shape = (16, 16)
@@ -160,10 +224,16 @@ def main(root: str):
         c0[f"{tag}_v_final"], c0[f"{tag}_w_final"] = states[-1].v, states[-1].w
         c0[f"{tag}_field"] = np.asarray(stim.field)
     np.savez_compressed(os.path.join(out, "config0.npz"), **c0)
+    config0_x64_fixtures(R64, out)
+    paramset_fixtures(R, R64, out)
     print("fixtures written to", out)
 
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=REFERENCE_ROOT)
-    main(ap.parse_args().reference)
+    ap.add_argument("--reference", default=REFERENCE_ROOT, required=REFERENCE_ROOT is None,
+                    help="reference checkout (default: $CARDIAX_REFERENCE)")
+    ap.add_argument("--only", default=None,
+                    help="regenerate one fixture group (paramsets, config0_x64)")
+    a = ap.parse_args()
+    main(a.reference, a.only)

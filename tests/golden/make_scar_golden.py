@@ -82,5 +82,6 @@ def main(root: str):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=REFERENCE_ROOT)
+    ap.add_argument("--reference", default=REFERENCE_ROOT, required=REFERENCE_ROOT is None,
+                    help="reference checkout (default: $CARDIAX_REFERENCE)")
     main(ap.parse_args().reference)

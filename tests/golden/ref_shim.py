@@ -28,7 +28,8 @@ import types
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("CARDIAX_REFERENCE", "/root/reference")
+# the reference checkout: set CARDIAX_REFERENCE (there is no default location)
+REFERENCE_ROOT = os.environ.get("CARDIAX_REFERENCE")
 
 
 def _jbool_class(float_t):
@@ -200,6 +201,8 @@ def load_reference(x64: bool = False, root: str = REFERENCE_ROOT):
     Returns a namespace with ``solve``, ``params``, ``stimulus`` and ``convert``.
     ``x64=True`` runs the same code in float64 (the reference with x64 enabled).
     """
+    if not root:
+        raise FileNotFoundError("no reference checkout: set CARDIAX_REFERENCE or pass root")
     if not os.path.isdir(os.path.join(root, "cardiax")):
         raise FileNotFoundError(f"reference checkout not found under {root}")
     float_t, int_t = (np.float64, np.int64) if x64 else (np.float32, np.int32)

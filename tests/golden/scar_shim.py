@@ -26,7 +26,8 @@ import types
 import numpy as np
 from scipy.signal import convolve2d as _sp_convolve2d
 
-REFERENCE_ROOT = os.environ.get("CARDIAX_REFERENCE", "/root/reference")
+# the reference checkout: set CARDIAX_REFERENCE (there is no default location)
+REFERENCE_ROOT = os.environ.get("CARDIAX_REFERENCE")
 
 
 class Tape:
@@ -189,6 +190,8 @@ def _polygon(r, c, shape=None):
 
 def load_utils_scars(tape: Tape, root: str = REFERENCE_ROOT):
     """The reference's ``deepx/utils_scars.py`` module, bound to the scripted ``tape``."""
+    if not root:
+        raise FileNotFoundError("no reference checkout: set CARDIAX_REFERENCE or pass root")
     path = os.path.join(root, "deepx", "utils_scars.py")
     if not os.path.isfile(path):
         raise FileNotFoundError(f"reference checkout not found under {root}")

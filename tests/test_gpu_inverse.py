@@ -1,0 +1,152 @@
+"""The differentiable inverse problem at its stated sizes: a 1e4-step 512^2 rollout through the
+sqrt(T) checkpointed adjoint (memory), the batched gradient at 256^2 against central finite
+differences of the float64 C oracle on 32 seeded D entries, and Adam on D.
+
+Finite differences (eps = 1e-3 relative) need a smooth loss: the regime is sub-threshold (u
+below the gate threshold V_c everywhere, so no Heaviside gate flips between the perturbed
+runs; a flip makes the loss jump, and a difference quotient across a jump is no derivative).
+Bar: each entry within 1e-3 of the finite difference, relative to max(|fd|, 1e-3 max|grad|).
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+P3 = (3.33, 19.6, 1250, 870, 41, 0.25, 12.5, 33.33, 29, 10, 0.85, 0.13, 0.04, 1)
+
+
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+
+
+def _smooth(rng, shape, lo, hi):
+    H, W = shape
+    i, j = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    f = np.zeros(shape)
+    for _ in range(4):
+        ci, cj, s = rng.uniform(0, H), rng.uniform(0, W), rng.uniform(0.1, 0.3) * max(H, W)
+        f += rng.uniform(-1, 1) * np.exp(-((i - ci) ** 2 + (j - cj) ** 2) / (2 * s * s))
+    f = (f - f.min()) / (f.max() - f.min() + 1e-12)
+    return lo + (hi - lo) * f
+
+
+def test_rollout_512_1e4_steps_keeps_sqrt_t_states():
+    """1e4 Euler steps at 512^2 with a travelling wave: the reverse pass holds ceil(sqrt(T))
+    checkpoints plus one recomputed segment (about 200 states of 3 MiB), not 1e4 states."""
+    _gpu()
+    from cardiax_gb300.adjoint import rollout
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    dev = torch.device("cuda", 0)
+    H = W = 512
+    T = 10000
+    f = np.zeros((H, W), np.float32)
+    f[:, :8] = 20.0
+    D = torch.full((H, W), 1e-3, device=dev, requires_grad=True)
+    th = torch.tensor(P3[:13], dtype=torch.float32, device=dev, requires_grad=True)
+    v0 = torch.ones((H, W), device=dev)
+    u0 = torch.zeros((H, W), device=dev, requires_grad=True)
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats(dev)
+    base = torch.cuda.memory_allocated(dev)
+    out = rollout(v0, v0.clone(), u0, D, th, [Stimulus(Protocol(0, 2, 1e9), f)], 0, T, [T])
+    loss = (out[0, 2] ** 2).mean()
+    loss.backward()
+    torch.cuda.synchronize()
+    peak = torch.cuda.max_memory_allocated(dev) - base
+    state_bytes = 3 * H * W * 4
+    K = math.ceil(math.sqrt(T))
+    print(f"512^2 x 1e4 steps: peak {peak / 2**20:.0f} MiB = {peak / state_bytes:.1f} states "
+          f"(checkpoints + segment = {2 * K}; all states would be {T})")
+    assert peak <= (2 * K + 24) * state_bytes
+    assert float(out[0, 2].max()) > 0.5  # the wave is still on the grid
+    for g in (D.grad, th.grad, u0.grad):
+        assert g is not None and bool(torch.isfinite(g).all())
+    assert float(D.grad.abs().max()) > 0
+
+
+def test_batched_gradient_matches_float64_finite_differences_256():
+    """rollout_batch at 256^2 (2 experiments sharing D, 400 steps, observations at 3 steps,
+    MSE against observations made with another D) vs central differences of the float64 C
+    oracle on 32 seeded D entries."""
+    _gpu()
+    import fk_oracle_c as C
+    from cardiax_gb300.adjoint import rollout_batch
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    dev = torch.device("cuda", 0)
+    H = W = 256
+    B, obs = 2, [100, 250, 400]
+    rng = np.random.default_rng(17)
+    D = _smooth(rng, (H, W), 3e-4, 1e-3)
+    D_obs = D * (1.0 + 0.2 * _smooth(rng, (H, W), -1.0, 1.0))
+    s0 = np.stack([np.stack([_smooth(rng, (H, W), 0.8, 1.0), _smooth(rng, (H, W), 0.8, 1.0),
+                             _smooth(rng, (H, W), 0.0, 0.09)]) for _ in range(B)])
+    fields = []
+    for b in range(B):
+        f = np.zeros((H, W))
+        r, c = int(rng.integers(20, H - 30)), int(rng.integers(20, W - 30))
+        f[r:r + 6, c:c + 6] = 0.5  # sub-threshold: u stays below V_c
+        fields.append(f)
+    protos = [(3, 2, 1e9), (40, 2, 1e9)]
+    stims = [[Stimulus(Protocol(*protos[b]), fields[b].astype(np.float32))] for b in range(B)]
+    th = torch.tensor(P3[:13], dtype=torch.float32, device=dev)
+    s0t = torch.tensor(s0, dtype=torch.float32, device=dev)
+    with torch.no_grad():
+        target = rollout_batch(s0t, torch.tensor(D_obs, dtype=torch.float32, device=dev), th,
+                               stims, 0, obs[-1], obs)[:, :, 2]
+    Dt = torch.tensor(D, dtype=torch.float32, device=dev, requires_grad=True)
+    out = rollout_batch(s0t, Dt, th, stims, 0, obs[-1], obs)
+    assert float(out[:, :, 2].max()) < P3[11]  # sub-threshold throughout the observations
+    ((out[:, :, 2] - target) ** 2).mean().backward()
+    got = Dt.grad.double().cpu().numpy()
+    tgt = target.double().cpu().numpy()
+    threads = C.max_threads()
+
+    def loss(Dm):
+        L = 0.0
+        for b in range(B):
+            st = tuple(s0[b, k] for k in range(3))
+            tcur = 0
+            for k, to in enumerate(obs):
+                st = C.forward_euler(st, tcur, to, P3, Dm, [(*protos[b], fields[b])], 0.01, 0.01,
+                                     threads=threads)
+                tcur = to
+                L += float(((st[2] - tgt[b, k]) ** 2).sum())
+        return L / (B * len(obs) * H * W)
+
+    worst = 0.0
+    scale = np.abs(got).max()
+    for _ in range(32):
+        i, j = int(rng.integers(0, H)), int(rng.integers(0, W))
+        eps = 1e-3 * D[i, j]
+        Dp, Dm = D.copy(), D.copy()
+        Dp[i, j] += eps
+        Dm[i, j] -= eps
+        fd = (loss(Dp) - loss(Dm)) / (2 * eps)
+        err = abs(got[i, j] - fd) / max(abs(fd), 1e-3 * scale)
+        worst = max(worst, err)
+        assert err <= 1e-3, (i, j, got[i, j], fd, err)
+    print(f"256^2 batched gradient vs float64 finite differences, 32 D entries: worst {worst:.2e}")
+
+
+def test_inverse_problem_adam_reduces_the_loss():
+    """The inverse problem at its stated size (16 experiments x 256^2, 5000 steps, 20
+    observations, point stimuli starting waves, scar ground truth): 30 Adam iterations on D
+    from a uniform D lower the loss and the error of D."""
+    _gpu()
+    import bench
+    from cardiax_gb300.adjoint import fit_diffusivity
+    dev = torch.device("cuda", 0)
+    s0, D_true, theta, stims, obs_t, obs = bench.inverse_problem(dev)
+    D0 = torch.full_like(D_true, 1e-3)
+    D, losses = fit_diffusivity(s0, D0, theta, stims, 0, obs_t[-1], obs_t, obs, iterations=30)
+    rel = lambda X: float((X - D_true).norm() / D_true.norm())  # noqa: E731
+    print(f"inverse problem, 30 Adam iterations: loss {losses[0]:.4g} -> {losses[-1]:.4g} "
+          f"(min {min(losses):.4g}); |D - D_true| / |D_true| {rel(D0):.3f} -> {rel(D):.3f}")
+    assert all(math.isfinite(x) for x in losses)
+    assert min(losses[-5:]) < losses[0]
+    assert rel(D) < rel(D0)

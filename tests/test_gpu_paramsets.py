@@ -1,0 +1,103 @@
+"""GPU parity beyond parameter set 3: the sets the batched workload draws (1A, 4A, 5) and a set
+with MAXFLOAT entries (2), against the reference's own forward, and a sample of the batched
+workload itself against the C oracle (not against the single-tissue GPU path).
+
+Bars (float32): max|du| <= 1e-4 at every checkpoint of 1000 steps against the reference's
+float32 run; against its float64 (x64) run the GPU must be as close as the reference's own
+float32 run is, within the same 1e-4 (under sets 1A/4A/5 the float32 parameters alone put the
+reference's float32 run 1.4e-4 .. 5.8e-4 away from its float64 run at 1000 steps).
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+TOL_U = 1e-4
+PARAMSET_CASES = ("1A", "4A", "5", "2")
+
+
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("name", PARAMSET_CASES)
+def test_paramset_forward_vs_reference(golden, name):
+    _gpu()
+    from cardiax_gb300 import params as Pm, solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    g = golden("paramsets.npz")
+    P = getattr(Pm, f"PARAMSET_{name}")
+    ck = [int(c) for c in g["checkpoints"]]
+    stims = [Stimulus(Protocol(0, 2, 1e9), g["f1"]), Stimulus(Protocol(300, 2, 1e9), g["f2"])]
+    states = solve.forward(solve.init(g["D"].shape), ck, P, g["D"], stims, 0.01, 0.01)
+    assert len(states) == len(ck) - 1
+    worst = 0.0
+    for c, s in zip(ck[1:], states):
+        e = float(np.abs(_np(s.u) - g[f"{name}_f32_u_{c}"]).max())
+        worst = max(worst, e)
+        assert e <= TOL_U, (name, c, e)
+    last = states[-1]
+    for var in "vw":
+        e = float(np.abs(_np(getattr(last, var)) - g[f"{name}_f32_{var}_{ck[-1]}"]).max())
+        assert e <= TOL_U, (name, var, e)
+    e64 = float(np.abs(_np(last.u) - g[f"{name}_f64_u_{ck[-1]}"]).max())
+    r64 = float(np.abs(g[f"{name}_f32_u_{ck[-1]}"] - g[f"{name}_f64_u_{ck[-1]}"]).max())
+    print(f"set {name}: max|du| vs ref32 over checkpoints {worst:.3g}; at 1000 steps "
+          f"|gpu-ref64| {e64:.3g}, |ref32-ref64| {r64:.3g}")
+    assert e64 <= r64 + TOL_U
+    assert float(last.u.max()) > 0.8  # a wave is travelling
+
+
+def _batched_sample(n=16, window=400):
+    """``n`` tissues of the batched workload (bench.batched_workload) covering as many
+    (parameter set, shape) pairs as possible, their stimulus starts folded into [0, window) so
+    that every tissue is stimulated within the 1000 steps."""
+    import bench
+    spec = bench.batched_workload()
+    seen, out = set(), []
+    for shape, P, D, f, proto in spec:
+        key = (tuple(P), shape)
+        if key in seen:
+            continue
+        seen.add(key)
+        out.append((shape, P, D, f, (proto[0] % window, proto[1], proto[2])))
+        if len(out) == n:
+            break
+    return out
+
+
+def test_batched_workload_sample_vs_c_oracle():
+    """16 tissues of the mixed batch (sets 1A/3/4A/5, sizes 64^2 .. 512^2 and 256x1024, scar D
+    maps, plane or point stimuli), 1000 steps in one batch, each tissue against the C oracle."""
+    _gpu()
+    import fk_oracle as O
+    import fk_oracle_c as C
+    from cardiax_gb300.batch import TissueBatch
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    from cardiax_gb300.tissue import Tissue
+    sample = _batched_sample()
+    assert len({tuple(s[1]) for s in sample}) == 4 and len({s[0] for s in sample}) == 5
+    tissues = [Tissue(shape, P, D, [Stimulus(Protocol(*proto), f)]) for shape, P, D, f, proto
+               in sample]
+    batch = TissueBatch(tissues, graph_steps=64)
+    batch.advance(0, 1000)
+    torch.cuda.synchronize()
+    threads = C.max_threads()
+    worst = 0.0
+    for t, (shape, P, D, f, proto) in zip(tissues, sample):
+        ref = C.forward_euler(O.init(shape), 0, 1000, P, D, [(*proto, f)], 0.01, 0.01,
+                              threads=threads)
+        got = [_np(x) for x in t.view()]
+        for var, a, b in zip("vwu", got, ref):
+            e = float(np.abs(a - b).max())
+            if var == "u":
+                worst = max(worst, e)
+            assert e <= TOL_U, (shape, P[:2], var, e)
+    batch.close()
+    print(f"batched sample (16 tissues, 1000 steps): max|du| vs the C oracle {worst:.3g}")

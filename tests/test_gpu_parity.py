@@ -292,3 +292,27 @@ def test_activation_times_within_one_step():
     assert d.max() <= min(max(1, spread), 4)
     dl = np.abs(gl - last)[both]
     assert (dl <= 1).mean() >= 0.99 and dl.max() <= 4
+
+
+def test_forward_dimensional_vs_oracle():
+    """forward_dimensional (cardiax/solve.py:133-165): the grid from the tissue size, the
+    checkpoints arange(0, int(final_time/dt), int(ms_step/dt)) -- the stop excluded, the
+    initial state not returned -- against the oracle's forward on those checkpoints."""
+    _gpu()
+    from cardiax_gb300 import convert, solve
+    from cardiax_gb300.stimulus import Direction, Protocol, linear
+    size, final_time, ms_step, dt, dx = (0.64, 0.8), 5.0, 1.0, 0.01, 0.01
+    shape = convert.realsize_to_shape(size, dx)
+    assert shape == (64, 80)
+    rng = np.random.default_rng(11)
+    D = _smooth(rng, shape, 4e-4, 1e-3)
+    stim = linear(shape, Direction.WEST, 0.15, 20.0, Protocol(0, 2, 1e9))
+    states = solve.forward_dimensional(size, final_time, ms_step, P3, D, [stim], dt, dx)
+    ck = list(range(0, int(final_time / dt), int(ms_step / dt)))
+    assert ck == [0, 100, 200, 300, 400] and len(states) == len(ck) - 1
+    ref = O.forward(O.init(shape), ck, P3, D, [O.OStim(0, 2, 1e9, _np(stim.field))], dt, dx)
+    for s, r in zip(states, ref):
+        for var in "vwu":
+            e = float(np.abs(_np(getattr(s, var)) - getattr(r, var)).max())
+            assert e <= TOL_U_1000, (var, e)
+    assert float(states[-1].u.max()) > 0.8

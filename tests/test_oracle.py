@@ -155,3 +155,55 @@ def test_rotate_field_matches_scipy(shape, angle):
     for a in (stripe, rng.uniform(0, 1, shape).astype(np.float32)):
         ref = rotate(a, angle=angle, mode="nearest", prefilter=False, reshape=False)
         np.testing.assert_allclose(O.rotate_field(a, angle), ref, rtol=1e-6, atol=1e-6)
+
+
+PARAMSET_CASES = ("1A", "4A", "5", "2")
+
+
+@pytest.mark.parametrize("name", PARAMSET_CASES)
+@pytest.mark.parametrize("tag,dtype", [("f32", np.float32), ("f64", np.float64)])
+def test_paramsets_golden(golden, name, tag, dtype):
+    """The oracle under parameter sets 1A, 4A, 5 and 2 (MAXFLOAT entries) against the
+    reference's own forward (tests/golden/make_golden.py), bit for bit."""
+    from cardiax_gb300 import params as Pm
+    g = golden("paramsets.npz")
+    P = getattr(Pm, f"PARAMSET_{name}")
+    ck = [int(c) for c in g["checkpoints"]]
+    stims = [O.OStim(0, 2, 1e9, g["f1"].astype(dtype)), O.OStim(300, 2, 1e9, g["f2"].astype(dtype))]
+    states = O.forward(O.init(g["D"].shape, dtype), ck, P, g["D"].astype(dtype), stims, 0.01,
+                       0.01)
+    for c, s in zip(ck[1:], states):
+        if f"{name}_{tag}_u_{c}" in g:
+            np.testing.assert_array_equal(s.u, g[f"{name}_{tag}_u_{c}"], err_msg=f"u at {c}")
+    np.testing.assert_array_equal(states[-1].v, g[f"{name}_{tag}_v_{ck[-1]}"])
+    np.testing.assert_array_equal(states[-1].w, g[f"{name}_{tag}_w_{ck[-1]}"])
+
+
+def test_autodiff_oracle_forward_equals_reference_x64(golden):
+    """The float64 torch restatement that stands in for jax.grad of the reference runs the
+    reference's own x64 forward (forward_small.npz, 200 steps on 32x40) to within 1e-12."""
+    import torch
+    import fk_torch as T
+    g = golden("forward_small.npz")
+    shp = g["D"].shape
+    f64 = lambda a: torch.as_tensor(np.asarray(a, np.float64))  # noqa: E731
+    st = (torch.ones(shp, dtype=torch.float64), torch.ones(shp, dtype=torch.float64),
+          torch.zeros(shp, dtype=torch.float64))
+    theta = f64(P3[:13])
+    stims = [(0, 2, 1e9, f64(g["f1"])), (60, 3, 1e9, f64(g["f2"]))]
+    with torch.no_grad():
+        v, w, u = T.forward(st, 0, 200, theta, P3[13], f64(g["D"]), stims, 0.01, 0.01)
+    for name, arr in zip("vwu", (v, w, u)):
+        err = float(np.abs(arr.numpy() - g[f"{name}_f64"]).max())
+        assert err <= 1e-12, f"{name}: {err}"
+
+
+def test_config0_x64_golden(golden):
+    """The configuration-0 runs in float64 (the reference with x64) at 1000 steps, bit for bit."""
+    g = golden("config0_x64.npz")
+    for tag, amp, proto in (("plain", 1.0, (0, 200, 1e9)), ("excite", 20.0, (0, 2, 1e9))):
+        field = O.linear_field((128, 128), 3, 5 / 128, amp, dtype=np.float64)
+        D = np.full((128, 128), 0.001, np.float64)
+        s = O.forward_euler(O.init((128, 128), np.float64), 0, 1000, P3, D,
+                            [O.OStim(*proto, field)], 0.01, 0.01)
+        np.testing.assert_array_equal(s.u, g[f"{tag}_u_1000"], err_msg=tag)

@@ -72,6 +72,56 @@ def test_noalloc_matches_forward_euler_on_consecutive_calls():
     assert float(b[2, :, :W].max()) > 0.5  # the wave is travelling
 
 
+@pytest.mark.parametrize("H,W", [(512, 512), (1024, 256)])
+def test_noalloc_accepts_a_grid_exactly_at_its_capacity(H, W):
+    """H * pitch == 512 * 512: the largest grid the array holds, an odd step count (the result
+    is copied back from the array), bit for bit against fk_forward_euler."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    N, L, g, s0, D, stims = _setup(H, W)
+    assert g.H * g.pitch == MAX_CELLS
+    params = N.Params(*P3)
+    a, b = s0.clone(), s0.clone()
+    scratch = torch.empty_like(s0)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = L.fk_forward_euler(g, a.data_ptr(), scratch.data_ptr(), D.data_ptr(),
+                            ctypes.byref(params), stims, 2, 0, 41, 0.01, 0.01, stream)
+    assert rc == 0, L.fk_status_string(rc)
+    rc = L.fk_forward_euler_noalloc(g, b.data_ptr(), D.data_ptr(), ctypes.byref(params), stims,
+                                    2, 0, 41, 0.01, 0.01, stream)
+    assert rc == 0, L.fk_status_string(rc)
+    torch.cuda.synchronize()
+    torch.testing.assert_close(b[:, :, :W], a[:, :, :W], rtol=0, atol=0, equal_nan=True)
+
+
+def test_noalloc_leaves_the_row_padding_of_the_state_unchanged():
+    """After a call on another grid shape has filled the array, an odd step count (whose result
+    comes back from the array) returns the caller's padding columns as they were."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream().cuda_stream
+    N, L, g1, s1, D1, st1 = _setup(300, 301)  # pitch 304: fills the array's padding with data
+    params = N.Params(*P3)
+    rc = L.fk_forward_euler_noalloc(g1, s1.data_ptr(), D1.data_ptr(), ctypes.byref(params), st1,
+                                    2, 0, 31, 0.01, 0.01, stream)
+    assert rc == 0, L.fk_status_string(rc)
+    N, L, g, s0, D, stims = _setup(200, 250)  # pitch 252: two padding columns per row
+    s0[:, :, 250:] = -7.25  # a marker the kernels never write
+    a, b = s0.clone(), s0.clone()
+    scratch = torch.empty_like(s0)
+    rc = L.fk_forward_euler(g, a.data_ptr(), scratch.data_ptr(), D.data_ptr(),
+                            ctypes.byref(params), stims, 2, 0, 33, 0.01, 0.01, stream)
+    assert rc == 0, L.fk_status_string(rc)
+    rc = L.fk_forward_euler_noalloc(g, b.data_ptr(), D.data_ptr(), ctypes.byref(params), stims,
+                                    2, 0, 33, 0.01, 0.01, stream)
+    assert rc == 0, L.fk_status_string(rc)
+    torch.cuda.synchronize()
+    torch.testing.assert_close(b[:, :, :250], a[:, :, :250], rtol=0, atol=0, equal_nan=True)
+    assert bool((b[:, :, 250:] == -7.25).all())
+
+
 def test_noalloc_refuses_grids_beyond_its_capacity():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
