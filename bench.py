@@ -242,8 +242,8 @@ def inverse_problem(dev, n_tissues: int = 16, steps: int = 5000, n_obs: int = 20
 
 def run_inverse(dev, iterations: int = 200, lr: float = 2e-5):
     """The inverse problem end to end: Adam on D (65,536 values) from a uniform D = 0.001,
-    ``iterations`` gradient evaluations of the 16 x 5000-step rollout (adjoint.fit_diffusivity),
-    D clipped to [1e-4, 2e-3] after each step."""
+    ``iterations`` gradient evaluations of the 16 x 5000-step rollout (adjoint.fit_diffusivity:
+    D the 2-cell Gaussian blur of the map Adam updates, clipped to [1e-4, 2e-3])."""
     import torch
     from cardiax_gb300.adjoint import fit_diffusivity
 
@@ -257,7 +257,7 @@ def run_inverse(dev, iterations: int = 200, lr: float = 2e-5):
     dt = time.perf_counter() - t0
     rel = lambda X: float((X - D_true).norm() / D_true.norm())  # noqa: E731
     drops = sum(1 for a, b in zip(losses, losses[1:]) if b < a)
-    return {"iterations": iterations, "optimizer": f"Adam(lr={lr:g}) on D, clip [1e-4, 2e-3]",
+    return {"iterations": iterations, "optimizer": f"Adam(lr={lr:g}) on D = blur_2cells(phi), phi clipped to [1e-4, 2e-3]",
             "seconds_per_iteration": dt / max(1, iterations),
             "loss_first": losses[0] if losses else None,
             "loss_last": losses[-1] if losses else None,

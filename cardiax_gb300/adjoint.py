@@ -370,34 +370,57 @@ def rollout_batch(states0, D, theta, stimuli_per_tissue, t0: int, t1: int,
                                int(t0), int(t1), list(obs_times), float(dt), float(dx), seg)
 
 
+def gaussian_blur(x: torch.Tensor, sigma_cells: float) -> torch.Tensor:
+    """A separable Gaussian blur of an (H, W) map (radius ceil(3 sigma), mirrored edges),
+    differentiable through torch (a constant map stays constant)."""
+    r = int(math.ceil(3.0 * sigma_cells))
+    if r < 1:
+        return x
+    k = torch.arange(-r, r + 1, dtype=torch.float32, device=x.device)
+    k = torch.exp(-k * k / (2.0 * sigma_cells * sigma_cells))
+    k = k / k.sum()
+    F = torch.nn.functional
+    y = F.conv2d(F.pad(x[None, None], (r, r, 0, 0), mode="reflect"), k.view(1, 1, 1, -1))
+    return F.conv2d(F.pad(y, (0, 0, r, r), mode="reflect"), k.view(1, 1, -1, 1))[0, 0]
+
+
 def fit_diffusivity(states0, D_init, theta, stimuli_per_tissue, t0: int, t1: int,
                     obs_times: Sequence[int], observations, iterations: int = 200,
-                    lr: float = 2e-5, bounds=(1e-4, 2e-3), dt: float = 0.01, dx: float = 0.01,
-                    Cm: float = 1.0, seg: int = None, callback=None):
+                    lr: float = 2e-5, bounds=(1e-4, 2e-3), smooth_cells: float = 2.0,
+                    dt: float = 0.01, dx: float = 0.01, Cm: float = 1.0, seg: int = None,
+                    callback=None):
     """The inverse problem: fits the per-cell diffusivity map to recordings of u.
 
     ``observations`` is (B, n_obs, H, W): u of B experiments (sharing D and the parameters
     ``theta``, each with its own initial state in ``states0`` (B, 3, H, W) and stimulus list)
     at ``obs_times``.  Each iteration runs :func:`rollout_batch` (forward, then the adjoint
     with sqrt(T) checkpoint-recompute), takes the mean squared error of u against the
-    observations, and makes one Adam step on D (learning rate ``lr``, in the units of D),
-    after which D is clipped to ``bounds`` (the explicit scheme needs D >= 0 and small enough
-    for stability).  ``callback(it, loss, D)`` is called after every step.  Returns the fitted
-    D and the list of losses (the loss of each iteration's D, before its step)."""
-    D = D_init.detach().clone().to(torch.float32).requires_grad_(True)
+    observations, and makes one Adam step (learning rate ``lr``, in the units of D).
+
+    D is the Gaussian blur (``smooth_cells`` cells; 0: none) of a free map that Adam updates
+    and that is clipped to ``bounds`` after each step: independent per-cell steps make D rough,
+    and on a rough D the explicit scheme -- its D_x u_x term and one-sided edge rows -- diverges
+    within a few hundred steps (as it does for per-cell noise in D), while the blurred map stays
+    smooth and inside the bounds (a blur of a clipped map is a convex combination).
+    ``callback(it, loss, D)`` is called after every step.  Returns the fitted D and the list of
+    losses (the loss of each iteration's D, before its step)."""
+    phi = D_init.detach().clone().to(torch.float32).requires_grad_(True)
     theta = theta.detach()
-    opt = torch.optim.Adam([D], lr=lr)
+    opt = torch.optim.Adam([phi], lr=lr)
+    to_D = (lambda f: gaussian_blur(f, smooth_cells)) if smooth_cells > 0 else (lambda f: f)
     losses = []
     for it in range(int(iterations)):
         opt.zero_grad(set_to_none=True)
+        D = to_D(phi)
         out = rollout_batch(states0, D, theta, stimuli_per_tissue, t0, t1, obs_times, dt, dx,
                             Cm, seg)
         loss = ((out[:, :, 2] - observations) ** 2).mean()
         loss.backward()
         opt.step()
         with torch.no_grad():
-            D.clamp_(float(bounds[0]), float(bounds[1]))
-        losses.append(float(loss))
+            phi.clamp_(float(bounds[0]), float(bounds[1]))
+        losses.append(float(loss.detach()))
         if callback is not None:
-            callback(it, losses[-1], D)
-    return D.detach(), losses
+            callback(it, losses[-1], D.detach())
+    with torch.no_grad():
+        return to_D(phi).detach(), losses

@@ -25,6 +25,7 @@ struct fk_batch {
     BatchMaps *d_maps = nullptr;
     BatchTissue *d_tissues = nullptr;
     BatchItem *d_items = nullptr;
+    int *d_ranges = nullptr;  // kBatchMaxGrid + 1 item offsets: CTA c runs [r[c], r[c+1])
     int *d_t = nullptr;
     int *status = nullptr;
     bool act = false;
@@ -32,6 +33,8 @@ struct fk_batch {
     std::vector<BatchMaps> h_maps;
     std::vector<BatchTissue> h_tissues;
     std::vector<BatchItem> h_items;
+    std::vector<int> h_ranges;
+    std::vector<uint8_t> h_edge;  // per item: an edge tile
     // captured graph
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -47,7 +50,7 @@ size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 int64_t tiles_of(const fk_grid &g) { return ((g.H + TY - 1) / TY) * ((g.W + TX - 1) / TX); }
 
 struct Layout {
-    size_t maps, tissues, items, t, total;
+    size_t maps, tissues, items, ranges, t, total;
 };
 
 Layout layout(int n, int64_t n_items) {
@@ -55,9 +58,34 @@ Layout layout(int n, int64_t n_items) {
     L.maps = 0;
     L.tissues = align_up(L.maps + sizeof(BatchMaps) * n);
     L.items = align_up(L.tissues + sizeof(BatchTissue) * n);
-    L.t = align_up(L.items + sizeof(BatchItem) * n_items);
+    L.ranges = align_up(L.items + sizeof(BatchItem) * n_items);
+    L.t = align_up(L.ranges + sizeof(int) * (kBatchMaxGrid + 1));
     L.total = align_up(L.t + 16);
     return L;
+}
+
+// Relative cost of an edge tile (clamped halo, one-sided rows, bounds checks) against an
+// interior one, for balancing the CTAs' runs of the work list.
+constexpr double kEdgeCost = 1.1;
+
+bool interior_tile(const fk_grid &g, int64_t i0, int64_t j0) {
+    return i0 >= BAND && i0 + TY <= g.H - BAND && j0 >= BAND && j0 + TX <= g.W - BAND;
+}
+
+// Cuts the work list into `grid` contiguous runs of about equal cost: r[c] .. r[c+1] for CTA c.
+void make_ranges(const std::vector<BatchItem> &items, const std::vector<uint8_t> &edge, int grid,
+                 std::vector<int> &r) {
+    const int n = (int)items.size();
+    double total = 0.0;
+    for (int k = 0; k < n; ++k) total += edge[k] ? kEdgeCost : 1.0;
+    r.assign(grid + 1, n);
+    r[0] = 0;
+    double acc = 0.0;
+    int c = 1;
+    for (int k = 0; k < n && c < grid; ++k) {
+        acc += edge[k] ? kEdgeCost : 1.0;
+        while (c < grid && acc >= total * c / grid) r[c++] = k + 1;
+    }
 }
 
 bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
@@ -123,6 +151,7 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
     b->d_maps = reinterpret_cast<BatchMaps *>(ws + L.maps);
     b->d_tissues = reinterpret_cast<BatchTissue *>(ws + L.tissues);
     b->d_items = reinterpret_cast<BatchItem *>(ws + L.items);
+    b->d_ranges = reinterpret_cast<int *>(ws + L.ranges);
     b->d_t = reinterpret_cast<int *>(ws + L.t);
     b->h_maps.resize(n);
     b->h_tissues.resize(n);
@@ -181,25 +210,26 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
             return rc;
         }
     }
-    // work list: the edge tiles of every tissue (the costlier clamped-halo path) first, then the
-    // interior tiles, each group with the larger tissues first
-    for (int pass = 0; pass < 2; ++pass)
-        for (int k : order) {
-            const fk_grid &g = tissues[k].g;
-            for (int64_t i0 = 0; i0 < g.H; i0 += TY)
-                for (int64_t j0 = 0; j0 < g.W; j0 += TX) {
-                    const bool interior = i0 >= BAND && i0 + TY <= g.H - BAND && j0 >= BAND &&
-                                          j0 + TX <= g.W - BAND;
-                    if (interior == (pass == 1))
-                        b->h_items.push_back(BatchItem{k, (int32_t)i0, (int32_t)j0, 0});
-                }
-        }
+    // work list: tissue by tissue (larger tissues first), each tissue's tiles row by row, so that
+    // a CTA's contiguous run of items changes tissue rarely; the runs are balanced by cost
+    for (int k : order) {
+        const fk_grid &g = tissues[k].g;
+        for (int64_t i0 = 0; i0 < g.H; i0 += TY)
+            for (int64_t j0 = 0; j0 < g.W; j0 += TX) {
+                b->h_items.push_back(BatchItem{k, (int32_t)i0, (int32_t)j0, 0});
+                b->h_edge.push_back(interior_tile(g, i0, j0) ? 0 : 1);
+            }
+    }
+    if (b->grid > kBatchMaxGrid) b->grid = kBatchMaxGrid;
+    make_ranges(b->h_items, b->h_edge, b->grid, b->h_ranges);
     cudaStream_t s = (cudaStream_t)stream;
     if (cudaMemcpyAsync(b->d_maps, b->h_maps.data(), sizeof(BatchMaps) * n,
                         cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(BatchTissue) * n,
                         cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaMemcpyAsync(b->d_items, b->h_items.data(), sizeof(BatchItem) * b->n_items,
+                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(b->d_ranges, b->h_ranges.data(), sizeof(int) * b->h_ranges.size(),
                         cudaMemcpyHostToDevice, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess) {
         delete b;
@@ -211,7 +241,17 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
 
 int fk_batch_set_grid(fk_batch *b, int ctas) {
     if (!b) return FK_ERR_NULL;
-    if (ctas < 1) return FK_ERR_ARGUMENT;
+    if (ctas < 1 || ctas > kBatchMaxGrid) return FK_ERR_ARGUMENT;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev != b->device) return FK_ERR_CUDA;
+    std::vector<int> r;
+    make_ranges(b->h_items, b->h_edge, ctas, r);
+    // ordered after the plan's earlier work on the legacy stream; the host copy stays alive
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(b->d_ranges, r.data(), sizeof(int) * r.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+        return FK_ERR_CUDA;
+    b->h_ranges.swap(r);
     b->grid = ctas;
     release_graph(b);
     return FK_OK;
@@ -219,8 +259,9 @@ int fk_batch_set_grid(fk_batch *b, int ctas) {
 
 static int launch_steps(fk_batch *b, int count, cudaStream_t s) {
     for (int k = 0; k < count; ++k) {
-        cudaError_t e = launch_batch_step(b->d_tissues, b->d_maps, b->d_items, b->n_items, b->d_t,
-                                          k, k & 1, b->act, b->status, b->grid, s);
+        cudaError_t e = launch_batch_step(b->d_tissues, b->d_maps, b->d_items, b->d_ranges,
+                                          b->n_items, b->d_t, k, k & 1, b->act, b->status,
+                                          b->grid, s);
         if (e != cudaSuccess) return FK_ERR_CUDA;
     }
     return launch_add_int(b->d_t, count, s) == cudaSuccess ? FK_OK : FK_ERR_CUDA;
@@ -272,8 +313,8 @@ int fk_batch_forward_euler(fk_batch *b, int64_t t0, int64_t t1, int graph_steps,
         if (n >= G) {
             if (!b->exec || b->graph_steps != G || b->graph_grid != b->grid) {
                 if ((rc = launch_steps(b, 0, s))) return rc;  // configures the kernel
-                if (launch_batch_step(b->d_tissues, b->d_maps, b->d_items, 0, b->d_t, 0, 0,
-                                      b->act, b->status, b->grid, s) != cudaSuccess)
+                if (launch_batch_step(b->d_tissues, b->d_maps, b->d_items, b->d_ranges, 0,
+                                      b->d_t, 0, 0, b->act, b->status, b->grid, s) != cudaSuccess)
                     return FK_ERR_CUDA;
                 if ((rc = ensure_graph(b, G))) return rc;
             }
@@ -322,8 +363,9 @@ int fk_batch_recompute(fk_batch *b, int64_t s, int64_t n, float *bufs, int64_t e
     if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;
     for (int64_t k = 1; k < n; ++k) {
         // step s+k-1 reads buffer (k-1)&1 and leaves x_{s+k} in buffer k&1
-        if (launch_batch_step(b->d_tissues, b->d_maps, b->d_items, b->n_items, b->d_t, (int)(k - 1),
-                              (int)((k - 1) & 1), false, b->status, b->grid, cs) != cudaSuccess)
+        if (launch_batch_step(b->d_tissues, b->d_maps, b->d_items, b->d_ranges, b->n_items,
+                              b->d_t, (int)(k - 1), (int)((k - 1) & 1), false, b->status, b->grid,
+                              cs) != cudaSuccess)
             return FK_ERR_CUDA;
         batch_state_out_kernel<<<cgrid, 256, 0, cs>>>(b->d_tissues, (int)(k & 1), bufs + k * ns,
                                                       exp_stride, ns);

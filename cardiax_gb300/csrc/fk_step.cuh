@@ -116,11 +116,15 @@ struct BatchItem {
 
 constexpr int SMEM_BATCH_BYTES = SMEM_STEP_DIRECT_BYTES + SMEM_ARGS_BYTES;  // two argument slots
 
-// One Euler step of every tissue: persistent CTAs drain `items`; the step index is
-// *t_dev + t_offset (so that a captured graph can be replayed for successive steps).
+// One Euler step of every tissue: CTA c (of `grid`) processes items[ranges[c] ..
+// ranges[c+1]); the step index is *t_dev + t_offset (so that a captured graph can be replayed
+// for successive steps).  n_items == 0 only configures the kernel (no launch).
 cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
-                              const BatchItem *items, int n_items, const int *t_dev, int t_offset,
-                              int parity, bool act, int *status, int grid, cudaStream_t stream);
+                              const BatchItem *items, const int *ranges, int n_items,
+                              const int *t_dev, int t_offset, int parity, bool act, int *status,
+                              int grid, cudaStream_t stream);
+// The most CTAs a batched launch may use (the size of a plan's range table).
+constexpr int kBatchMaxGrid = 4096;
 // *p += v (advances the step counter of a captured graph).
 cudaError_t launch_add_int(int *p, int v, cudaStream_t stream);
 // Copies buffer 1 (scratch) of every tissue back to buffer 0 (state).

@@ -291,7 +291,13 @@ __global__ void __launch_bounds__(S_NT, S_CTAS_PER_SM)
         }
         const bool ok = mbar_wait_bounded(&bar[s], (n / S_NSTAGE) & 1);
         if (__syncthreads_or(!ok)) {
-            if (tid == 0) atomicOr(a.status, kStatusTimeout);
+            if (tid == 0) {
+                atomicOr(a.status, kStatusTimeout);
+                // tiles n .. n + S_NSTAGE - 2 may still be loading: wait (bounded) for them
+                for (int q = 0; q < S_NSTAGE - 1; ++q)
+                    if (tile + q * (int)gridDim.x < ntiles)
+                        mbar_wait_bounded(&bar[(n + q) % S_NSTAGE], ((n + q) / S_NSTAGE) & 1);
+            }
             return;
         }
         // every warp has finished tile n-1, whose stage now takes tile n + S_NSTAGE - 1

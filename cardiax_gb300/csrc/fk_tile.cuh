@@ -339,9 +339,16 @@ static __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_ro
 struct NoHook {
     __device__ void operator()() const {}
 };
+// The per-tissue pair constants of the packed path: 1/dx and dt, each held twice.  A one-tissue
+// launch passes the fields of its PackConsts parameter (constant-bank operands after inlining);
+// the batched kernel passes its current tissue's values in registers.
+struct PairScale {
+    float2 rdx, dt;
+};
 template <bool DERIV, bool ACT, bool EDGE, bool PK, bool DIRECT = false, int HEUN = 0, class P1,
           class P2 = NoHook>
-__device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts *pk, float t,
+__device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts *pk, PairScale ps,
+                                             float t,
                                              const Stage &st, float *sux, float *suy,
                                              const TileIO &io, unsigned active, int i0, int j0,
                                              P1 &&after_pass1, bool ok = true,
@@ -375,7 +382,7 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                 o = q_head(kc, ld_quad(b), ld_quad(b + SW), ld_quad(b + 2 * SW), ld_quad(b + 3 * SW));
             else
                 o = q_tail(kc, ld_quad(b - 3 * SW), ld_quad(b - 2 * SW), ld_quad(b - SW), ld_quad(b));
-            o = q_scale(o, kc.rdx);
+            o = q_scale(o, ps.rdx);
             st4(sux + r * TX + 4 * q, make_float4(o.lo.x, o.lo.y, o.hi.x, o.hi.y));
             continue;
         }
@@ -414,8 +421,8 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
         float o[4];
         if constexpr (PK) {
             const PackConsts &kc = *pk;  // u_y at columns c .. c+3 as the pairs (c, c+1), (c+2, c+3)
-            const float2 lo = p_mul(pg_central_row(kc, e[2], e[3], e[4], e[5], e[6], e[7]), kc.rdx);
-            const float2 hi = p_mul(pg_central_row(kc, e[4], e[5], e[6], e[7], e[8], e[9]), kc.rdx);
+            const float2 lo = p_mul(pg_central_row(kc, e[2], e[3], e[4], e[5], e[6], e[7]), ps.rdx);
+            const float2 hi = p_mul(pg_central_row(kc, e[4], e[5], e[6], e[7], e[8], e[9]), ps.rdx);
             o[0] = lo.x;
             o[1] = lo.y;
             o[2] = hi.x;
@@ -495,8 +502,8 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                 uxx = q_tail(kc, ux3, uxr[o - 2], uxr[o - 1], uxc);
                 dxD = q_tail(kc, d3, dxr[o - 2], dxr[o - 1], dcq);
             }
-            uxx = q_scale(uxx, kc.rdx);
-            dxD = q_scale(dxD, kc.rdx);
+            uxx = q_scale(uxx, ps.rdx);
+            dxD = q_scale(dxD, ps.rdx);
             const float *yb = suy + r * SW + 4 * tx;
             const float4 y0 = ld4(yb), y1 = ld4(yb + 4), y2 = ld4(yb + 8);
             const float4 dl = ld4(db - 4), dr = ld4(db + 4);
@@ -506,10 +513,10 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                                  y2.x, y2.y, y2.z, y2.w};  // u_y at columns j-4 .. j+7
             const float g[12] = {dl.x, dl.y, dl.z, dl.w, dcq.lo.x, dcq.lo.y, dcq.hi.x, dcq.hi.y,
                                  dr.x, dr.y, dr.z, dr.w};  // D at columns j-4 .. j+7
-            float2 uyy_lo = p_mul(pg_central_row(kc, f[2], f[3], f[4], f[5], f[6], f[7]), kc.rdx);
-            float2 uyy_hi = p_mul(pg_central_row(kc, f[4], f[5], f[6], f[7], f[8], f[9]), kc.rdx);
-            float2 dyD_lo = p_mul(pg_central_row(kc, g[2], g[3], g[4], g[5], g[6], g[7]), kc.rdx);
-            float2 dyD_hi = p_mul(pg_central_row(kc, g[4], g[5], g[6], g[7], g[8], g[9]), kc.rdx);
+            float2 uyy_lo = p_mul(pg_central_row(kc, f[2], f[3], f[4], f[5], f[6], f[7]), ps.rdx);
+            float2 uyy_hi = p_mul(pg_central_row(kc, f[4], f[5], f[6], f[7], f[8], f[9]), ps.rdx);
+            float2 dyD_lo = p_mul(pg_central_row(kc, g[2], g[3], g[4], g[5], g[6], g[7]), ps.rdx);
+            float2 dyD_hi = p_mul(pg_central_row(kc, g[4], g[5], g[6], g[7], g[8], g[9]), ps.rdx);
             if (EDGE && (j == 0 || (j <= W - 1 && W - 1 <= j + 3))) {
                 // the one-sided rows at column 0 (head) and W-1 (tail), second derivative / D_y
                 float uy4[4] = {uyy_lo.x, uyy_lo.y, uyy_hi.x, uyy_hi.y};
@@ -590,12 +597,12 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                 nu_lo = p_fma(p_add(mk2(du1.x, du1.y), du_lo), hh, mk2(xu.x, xu.y));
                 nu_hi = p_fma(p_add(mk2(du1.z, du1.w), du_hi), hh, mk2(xu.z, xu.w));
             } else {
-                nv_lo = p_fma(rl.dv, kc.dt, v_lo);
-                nv_hi = p_fma(rh.dv, kc.dt, v_hi);
-                nw_lo = p_fma(rl.dw, kc.dt, w_lo);
-                nw_hi = p_fma(rh.dw, kc.dt, w_hi);
-                nu_lo = p_fma(du_lo, kc.dt, u_lo);
-                nu_hi = p_fma(du_hi, kc.dt, u_hi);
+                nv_lo = p_fma(rl.dv, ps.dt, v_lo);
+                nv_hi = p_fma(rh.dv, ps.dt, v_hi);
+                nw_lo = p_fma(rl.dw, ps.dt, w_lo);
+                nw_hi = p_fma(rh.dw, ps.dt, w_hi);
+                nu_lo = p_fma(du_lo, ps.dt, u_lo);
+                nu_hi = p_fma(du_hi, ps.dt, u_hi);
             }
             const float4 ov4 = make_float4(nv_lo.x, nv_lo.y, nv_hi.x, nv_hi.y);
             const float4 ow4 = make_float4(nw_lo.x, nw_lo.y, nw_hi.x, nw_hi.y);
@@ -790,21 +797,22 @@ template <bool DERIV, bool ACT, bool PK = false, bool DIRECT = false, int HEUN =
 __device__ __forceinline__ bool process_tile(const StepArgs &a, float t, const Stage &st,
                                              float *sux, float *suy, const TileIO &io,
                                              unsigned active, int i0, int j0, P1 &&after_pass1,
-                                             const PackConsts *pk = nullptr, bool ok = true,
+                                             const PackConsts *pk = nullptr,
+                                             PairScale ps = PairScale{}, bool ok = true,
                                              P2 &&after_barrier = P2{}) {
     const int H = a.H, W = a.W;
     const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
     if (interior) {
-        return compute_tile<DERIV, ACT, false, PK, DIRECT, HEUN>(a, pk, t, st, sux, suy, io, active,
+        return compute_tile<DERIV, ACT, false, PK, DIRECT, HEUN>(a, pk, ps, t, st, sux, suy, io, active,
                                                                  i0, j0, after_pass1, ok,
                                                                  after_barrier);
     } else if (!is_sliver(i0, j0, H, W)) {
-        return compute_tile<DERIV, ACT, true, PK, DIRECT, HEUN>(a, pk, t, st, sux, suy, io, active,
+        return compute_tile<DERIV, ACT, true, PK, DIRECT, HEUN>(a, pk, ps, t, st, sux, suy, io, active,
                                                                 i0, j0, after_pass1, ok,
                                                                 after_barrier);
     } else if (DIRECT) {
         // interior cells from the tile passes; the band cells per cell, straight to global memory
-        if (!compute_tile<DERIV, ACT, false, PK, DIRECT, HEUN>(a, pk, t, st, sux, suy, io, active,
+        if (!compute_tile<DERIV, ACT, false, PK, DIRECT, HEUN>(a, pk, ps, t, st, sux, suy, io, active,
                                                                i0, j0, after_pass1, ok,
                                                                after_barrier, true))
             return false;
@@ -812,7 +820,7 @@ __device__ __forceinline__ bool process_tile(const StepArgs &a, float t, const S
                                      OutTile{nullptr, nullptr, nullptr, i0, j0}, HEUN);
         return true;
     } else {
-        compute_tile<DERIV, false, false, PK>(a, pk, t, st, sux, suy, io, active, i0, j0,
+        compute_tile<DERIV, false, false, PK>(a, pk, ps, t, st, sux, suy, io, active, i0, j0,
                                               after_pass1);
         __syncthreads();  // every cell of this tile is recomputed below where needed
         boundary_band<ACT && !DERIV>(a, t, active, DERIV, i0, j0,

@@ -135,8 +135,9 @@ def _forward_euler_backward(ctx, grad):
     lam0 = adj.rollout_gradient(tis.state.clone(), t0, t1, [t1], g)
     g_params = torch.zeros(14, dtype=params.dtype, device=params.device)
     g_params[:13] = adj.grad_theta().to(device=params.device, dtype=params.dtype)
-    return (lam0[..., :W].contiguous(), adj.grad_D().clone().to(D.dtype), g_params, None, None,
-            None, None, None, None)
+    # one entry per input, the stimulus-field list answered with a list
+    return (lam0[..., :W].contiguous(), adj.grad_D().clone().to(D.dtype), g_params, None,
+            [None] * len(fields), None, None, None, None)
 
 
 torch.library.register_autograd(f"{NS}::forward_euler", _forward_euler_backward,
