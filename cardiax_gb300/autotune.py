@@ -1,6 +1,7 @@
 """Autotuners of the stepping configuration.
 
-``tune_batch``: for a batch, times on the batch's own tissues every ``graph_steps`` candidate
+``tune_batch``: for a batch, times on the batch's own tissues every combination of the tile
+geometry of the batched kernel (work items of 32 x 64 or 16 x 64 cells) and ``graph_steps``
 in {0, 16, 64, 256} (how many steps one captured CUDA graph replays) over a short run with CUDA
 events and keeps the fastest.
 
@@ -28,6 +29,7 @@ TISSUE_CANDIDATES = (("step", 1, 0), ("step", 1, 1), ("step", 2, 0), ("step", 4,
                      ("step", 8, 0), ("flow", 1, 0))
 
 GRAPH_CANDIDATES = (0, 16, 64, 256)
+TILE_ROW_CANDIDATES = (32, 16)
 
 
 def _signature(batch: TissueBatch):
@@ -36,29 +38,35 @@ def _signature(batch: TissueBatch):
 
 
 def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CANDIDATES,
-               verbose: bool = False) -> dict:
-    """Picks ``graph_steps`` for ``batch`` (stored on it) and returns the timings."""
-    key = (_signature(batch), trial_steps, tuple(candidates))
+               tile_rows=TILE_ROW_CANDIDATES, verbose: bool = False) -> dict:
+    """Picks the tile geometry and ``graph_steps`` for ``batch`` (set on it) and returns the
+    timings: ``{"tile_rows": r, "graph_steps": g, "ms_per_step": {(r, g): ms}}``."""
+    key = (_signature(batch), trial_steps, tuple(candidates), tuple(tile_rows))
     if key in _CACHE:
-        batch.graph_steps = _CACHE[key]["graph_steps"]
-        return _CACHE[key]
+        res = _CACHE[key]
+        batch.set_tile_rows(res["tile_rows"])
+        batch.graph_steps = res["graph_steps"]
+        return res
     saved = [(t.state.clone(), None if t.activation is None else
               (t.act_first.clone(), t.act_last.clone(), t.act_count.clone()))
              for t in batch.tissues]
     timings = {}
-    for g in candidates:
-        batch.advance(0, 2, graph_steps=0)  # warm-up
-        if g:
-            batch.advance(0, g, graph_steps=g)  # captures the graph outside the timed run
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        batch.advance(0, trial_steps, graph_steps=g)
-        e1.record()
-        torch.cuda.synchronize()
-        timings[g] = e0.elapsed_time(e1) / trial_steps
-        if verbose:
-            print(f"autotune graph_steps={g}: {timings[g] * 1e3:.1f} us/step")
+    for rows in tile_rows:
+        batch.set_tile_rows(rows)
+        for g in candidates:
+            batch.advance(0, 2, graph_steps=0)  # warm-up
+            if g:
+                batch.advance(0, g, graph_steps=g)  # captures the graph outside the timed run
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            batch.advance(0, trial_steps, graph_steps=g)
+            e1.record()
+            torch.cuda.synchronize()
+            timings[(rows, g)] = e0.elapsed_time(e1) / trial_steps
+            if verbose:
+                print(f"autotune tile_rows={rows} graph_steps={g}: "
+                      f"{timings[(rows, g)] * 1e3:.1f} us/step")
     for t, (st, act) in zip(batch.tissues, saved):
         t.state.copy_(st)
         if act is not None:
@@ -66,8 +74,9 @@ def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CAND
             t.act_last.copy_(act[1])
             t.act_count.copy_(act[2])
     best = min(timings, key=timings.get)
-    batch.graph_steps = best
-    res = {"graph_steps": best, "ms_per_step": timings}
+    batch.set_tile_rows(best[0])
+    batch.graph_steps = best[1]
+    res = {"tile_rows": best[0], "graph_steps": best[1], "ms_per_step": timings}
     _CACHE[key] = res
     return res
 

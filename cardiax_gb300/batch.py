@@ -20,7 +20,8 @@ class TissueBatch:
     """A batch of :class:`Tissue` objects on one device (shapes, parameters, D maps, stimuli and
     dt/dx may all differ).  ``advance(t0, t1)`` steps every tissue in place."""
 
-    def __init__(self, tissues: Sequence[Tissue], graph_steps: int = 64, ctas: int = None):
+    def __init__(self, tissues: Sequence[Tissue], graph_steps: int = 64, ctas: int = None,
+                 tile_rows: int = 32):
         if not tissues:
             raise ValueError("empty batch")
         dev = tissues[0].device
@@ -47,11 +48,20 @@ class TissueBatch:
         N.call("fk_batch_create", descs, len(tissues), base, nbytes, stream_handle(),
                ctypes.byref(plan))
         self._plan = plan
+        self.tile_rows = 32
         if ctas is not None:
             self.set_ctas(ctas)
+        if tile_rows != 32:
+            self.set_tile_rows(tile_rows)
 
     def set_ctas(self, ctas: int) -> "TissueBatch":
         N.call("fk_batch_set_grid", self._plan, int(ctas))
+        return self
+
+    def set_tile_rows(self, rows: int) -> "TissueBatch":
+        """Work items of ``rows`` x 64 cells (32 or 16); the results do not change."""
+        N.call("fk_batch_set_tile_rows", self._plan, int(rows))
+        self.tile_rows = int(rows)
         return self
 
     @property

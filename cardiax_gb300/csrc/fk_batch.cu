@@ -20,26 +20,49 @@
 
 using namespace fk;
 
+// The tile geometries the batched kernel is built for (fk_batch_rows32.cu, fk_batch_rows16.cu):
+// rows x 64 columns, u loaded with a 4-cell halo (rows + 8 rows), D with a 2-row halo.
+typedef cudaError_t (*BatchLaunchFn)(const void *, const void *, const void *, const int *, int,
+                                     const int *, int, int, bool, int *, int, cudaStream_t);
+cudaError_t fk_batch_launch_rows32(const void *, const void *, const void *, const int *, int,
+                                   const int *, int, int, bool, int *, int, cudaStream_t);
+cudaError_t fk_batch_launch_rows16(const void *, const void *, const void *, const int *, int,
+                                   const int *, int, int, bool, int *, int, cudaStream_t);
+namespace {
+struct TileShape {
+    int rows, cols, ctas_per_sm;
+    BatchLaunchFn launch;
+};
+constexpr int kShapes = 2;
+const TileShape kShape[kShapes] = {{32, 64, 2, fk_batch_launch_rows32},
+                                   {16, 64, 2, fk_batch_launch_rows16}};
+}  // namespace
+
 struct fk_batch {
-    int n = 0, n_items = 0, grid = 0, device = -1;
-    BatchMaps *d_maps = nullptr;
+    int n = 0, grid = 0, device = -1;
+    int shape = 0;  // index into kShape of the tile geometry in use
     BatchTissue *d_tissues = nullptr;
-    BatchItem *d_items = nullptr;
-    int *d_ranges = nullptr;  // kBatchMaxGrid + 1 item offsets: CTA c runs [r[c], r[c+1])
     int *d_t = nullptr;
     int *status = nullptr;
     bool act = false;
+    // per tile geometry: TMA maps (box heights differ), the work list and the CTAs' runs of it
+    struct PerShape {
+        BatchMaps *d_maps = nullptr;
+        BatchItem *d_items = nullptr;
+        int *d_ranges = nullptr;  // kBatchMaxGrid + 1 item offsets: CTA c runs [r[c], r[c+1])
+        int n_items = 0;
+        std::vector<BatchMaps> h_maps;
+        std::vector<BatchItem> h_items;
+        std::vector<uint8_t> h_edge;  // per item: an edge tile
+        std::vector<int> h_ranges;
+    } sp[kShapes];
     // host staging (kept alive until destroy: the uploads are asynchronous)
-    std::vector<BatchMaps> h_maps;
     std::vector<BatchTissue> h_tissues;
-    std::vector<BatchItem> h_items;
-    std::vector<int> h_ranges;
-    std::vector<uint8_t> h_edge;  // per item: an edge tile
     // captured graph
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    int graph_steps = 0, graph_grid = 0;
+    int graph_steps = 0, graph_grid = 0, graph_shape = 0;
 };
 
 namespace {
@@ -47,20 +70,32 @@ namespace {
 constexpr size_t kAlign = 128;
 size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
-int64_t tiles_of(const fk_grid &g) { return ((g.H + TY - 1) / TY) * ((g.W + TX - 1) / TX); }
+int64_t tiles_of(const fk_grid &g, int shape) {
+    const TileShape &t = kShape[shape];
+    return ((g.H + t.rows - 1) / t.rows) * ((g.W + t.cols - 1) / t.cols);
+}
 
 struct Layout {
-    size_t maps, tissues, items, ranges, t, total;
+    size_t maps[kShapes], tissues, items[kShapes], ranges[kShapes], t, total;
 };
 
-Layout layout(int n, int64_t n_items) {
+Layout layout(int n, const int64_t *n_items) {
     Layout L;
-    L.maps = 0;
-    L.tissues = align_up(L.maps + sizeof(BatchMaps) * n);
-    L.items = align_up(L.tissues + sizeof(BatchTissue) * n);
-    L.ranges = align_up(L.items + sizeof(BatchItem) * n_items);
-    L.t = align_up(L.ranges + sizeof(int) * (kBatchMaxGrid + 1));
-    L.total = align_up(L.t + 16);
+    size_t at = 0;
+    for (int k = 0; k < kShapes; ++k) {
+        L.maps[k] = at;
+        at = align_up(at + sizeof(BatchMaps) * n);
+    }
+    L.tissues = at;
+    at = align_up(at + sizeof(BatchTissue) * n);
+    for (int k = 0; k < kShapes; ++k) {
+        L.items[k] = at;
+        at = align_up(at + sizeof(BatchItem) * n_items[k]);
+        L.ranges[k] = at;
+        at = align_up(at + sizeof(int) * (kBatchMaxGrid + 1));
+    }
+    L.t = at;
+    L.total = align_up(at + 16);
     return L;
 }
 
@@ -68,8 +103,9 @@ Layout layout(int n, int64_t n_items) {
 // interior one, for balancing the CTAs' runs of the work list.
 constexpr double kEdgeCost = 1.1;
 
-bool interior_tile(const fk_grid &g, int64_t i0, int64_t j0) {
-    return i0 >= BAND && i0 + TY <= g.H - BAND && j0 >= BAND && j0 + TX <= g.W - BAND;
+bool interior_tile(const fk_grid &g, int shape, int64_t i0, int64_t j0) {
+    const TileShape &t = kShape[shape];
+    return i0 >= BAND && i0 + t.rows <= g.H - BAND && j0 >= BAND && j0 + t.cols <= g.W - BAND;
 }
 
 // Cuts the work list into `grid` contiguous runs of about equal cost: r[c] .. r[c+1] for CTA c.
@@ -104,8 +140,9 @@ extern "C" {
 
 size_t fk_batch_workspace_bytes(const fk_tissue *tissues, int n) {
     if (!tissues || n <= 0) return 0;
-    int64_t items = 0;
-    for (int k = 0; k < n; ++k) items += tiles_of(tissues[k].g);
+    int64_t items[kShapes] = {};
+    for (int k = 0; k < n; ++k)
+        for (int q = 0; q < kShapes; ++q) items[q] += tiles_of(tissues[k].g, q);
     return layout(n, items).total;
 }
 
@@ -114,7 +151,7 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
     if (!tissues || !workspace || !out) return FK_ERR_NULL;
     if (n <= 0 || n > (1 << 20)) return FK_ERR_ARGUMENT;
     if ((reinterpret_cast<uintptr_t>(workspace) & (kAlign - 1)) != 0) return FK_ERR_ALIGN;
-    int64_t n_items = 0;
+    int64_t n_items[kShapes] = {};
     bool any_act = false, all_act = true;
     for (int k = 0; k < n; ++k) {
         const fk_tissue &t = tissues[k];
@@ -127,17 +164,17 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
         if (a && (!t.act.first || !t.act.count)) return FK_ERR_NULL;
         any_act |= a;
         all_act &= a;
-        n_items += tiles_of(t.g);
+        for (int q = 0; q < kShapes; ++q) n_items[q] += tiles_of(t.g, q);
     }
     if (any_act && !all_act) return FK_ERR_ARGUMENT;  // tracking is all or nothing per batch
-    if (n_items > (int64_t(1) << 30)) return FK_ERR_SHAPE;
+    for (int q = 0; q < kShapes; ++q)
+        if (n_items[q] > (int64_t(1) << 30)) return FK_ERR_SHAPE;
     const Layout L = layout(n, n_items);
     if (bytes < L.total) return FK_ERR_ARGUMENT;
 
     fk_batch *b = new (std::nothrow) fk_batch();
     if (!b) return FK_ERR_ARGUMENT;
     b->n = n;
-    b->n_items = (int)n_items;
     b->act = any_act;
     b->status = status_ptr();
     if (!b->status || cudaGetDevice(&b->device) != cudaSuccess) {
@@ -146,40 +183,58 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
     }
     int n_sm = 0;
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, b->device);
-    b->grid = n_sm > 0 ? n_sm * CTAS_PER_SM : 1;
+    b->grid = n_sm > 0 ? n_sm * kShape[0].ctas_per_sm : 1;
+    if (b->grid > kBatchMaxGrid) b->grid = kBatchMaxGrid;
     char *ws = static_cast<char *>(workspace);
-    b->d_maps = reinterpret_cast<BatchMaps *>(ws + L.maps);
     b->d_tissues = reinterpret_cast<BatchTissue *>(ws + L.tissues);
-    b->d_items = reinterpret_cast<BatchItem *>(ws + L.items);
-    b->d_ranges = reinterpret_cast<int *>(ws + L.ranges);
     b->d_t = reinterpret_cast<int *>(ws + L.t);
-    b->h_maps.resize(n);
     b->h_tissues.resize(n);
-    b->h_items.reserve(n_items);
+    for (int q = 0; q < kShapes; ++q) {
+        fk_batch::PerShape &P = b->sp[q];
+        P.d_maps = reinterpret_cast<BatchMaps *>(ws + L.maps[q]);
+        P.d_items = reinterpret_cast<BatchItem *>(ws + L.items[q]);
+        P.d_ranges = reinterpret_cast<int *>(ws + L.ranges[q]);
+        P.n_items = (int)n_items[q];
+        P.h_maps.resize(n);
+        P.h_items.reserve(n_items[q]);
+        P.h_edge.reserve(n_items[q]);
+    }
 
     // tiles of the larger tissues first: the persistent CTAs then finish together
     std::vector<int> order(n);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-        return tiles_of(tissues[x].g) > tiles_of(tissues[y].g);
+        return tiles_of(tissues[x].g, 0) > tiles_of(tissues[y].g, 0);
     });
     for (int k = 0; k < n; ++k) {
         const fk_tissue &t = tissues[k];
         const int64_t plane = t.g.H * t.g.pitch;
         Stim st[kMaxStim];
         int rc = make_stims(t.stimuli, t.n_stimuli, t.g, st);
-        if (!rc) rc = make_plane_map(&b->h_maps[k].maps[0].d, t.D, t.g.H, t.g.W, t.g.pitch, SW, SD_H);
         const Model m = make_model(t.params);
+        // TMA maps per geometry: u with a 4-cell halo, D with a 2-row halo (columns: 4 cells)
+        for (int q = 0; q < kShapes && !rc; ++q) {
+            const TileShape &ts = kShape[q];
+            const int sw = ts.cols + 8, su_h = ts.rows + 8, sd_h = ts.rows + 4;
+            BatchMaps &bm = b->sp[q].h_maps[k];
+            if ((rc = make_plane_map(&bm.maps[0].d, t.D, t.g.H, t.g.W, t.g.pitch, sw, sd_h))) break;
+            for (int p = 0; p < 2 && !rc; ++p) {
+                const float *in = p ? t.scratch : t.state;
+                float *o = p ? t.state : t.scratch;
+                StepMaps &sm = bm.maps[p];
+                if (p) sm.d = bm.maps[0].d;
+                if ((rc = make_plane_map(&sm.u, in + 2 * plane, t.g.H, t.g.W, t.g.pitch, sw, su_h)) ||
+                    (rc = make_plane_map(&sm.ov, o, t.g.H, t.g.W, t.g.pitch, ts.cols, ts.rows)) ||
+                    (rc = make_plane_map(&sm.ow, o + plane, t.g.H, t.g.W, t.g.pitch, ts.cols,
+                                         ts.rows)) ||
+                    (rc = make_plane_map(&sm.ou, o + 2 * plane, t.g.H, t.g.W, t.g.pitch, ts.cols,
+                                         ts.rows)))
+                    break;
+            }
+        }
         for (int p = 0; p < 2 && !rc; ++p) {
             const float *in = p ? t.scratch : t.state;
             float *o = p ? t.state : t.scratch;
-            StepMaps &sm = b->h_maps[k].maps[p];
-            if (p) sm.d = b->h_maps[k].maps[0].d;
-            if ((rc = make_plane_map(&sm.u, in + 2 * plane, t.g.H, t.g.W, t.g.pitch, SW, SU_H)) ||
-                (rc = make_plane_map(&sm.ov, o, t.g.H, t.g.W, t.g.pitch, TX, TY)) ||
-                (rc = make_plane_map(&sm.ow, o + plane, t.g.H, t.g.W, t.g.pitch, TX, TY)) ||
-                (rc = make_plane_map(&sm.ou, o + 2 * plane, t.g.H, t.g.W, t.g.pitch, TX, TY)))
-                break;
             StepArgs &a = b->h_tissues[k].args[p];
             std::memset(&a, 0, sizeof(a));
             a.v = in;
@@ -210,28 +265,34 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
             return rc;
         }
     }
-    // work list: tissue by tissue (larger tissues first), each tissue's tiles row by row, so that
-    // a CTA's contiguous run of items changes tissue rarely; the runs are balanced by cost
-    for (int k : order) {
-        const fk_grid &g = tissues[k].g;
-        for (int64_t i0 = 0; i0 < g.H; i0 += TY)
-            for (int64_t j0 = 0; j0 < g.W; j0 += TX) {
-                b->h_items.push_back(BatchItem{k, (int32_t)i0, (int32_t)j0, 0});
-                b->h_edge.push_back(interior_tile(g, i0, j0) ? 0 : 1);
-            }
+    // work lists: tissue by tissue (larger tissues first), each tissue's tiles row by row, so
+    // that a CTA's contiguous run of items changes tissue rarely; the runs are balanced by cost
+    for (int q = 0; q < kShapes; ++q) {
+        fk_batch::PerShape &P = b->sp[q];
+        const TileShape &ts = kShape[q];
+        for (int k : order) {
+            const fk_grid &g = tissues[k].g;
+            for (int64_t i0 = 0; i0 < g.H; i0 += ts.rows)
+                for (int64_t j0 = 0; j0 < g.W; j0 += ts.cols) {
+                    P.h_items.push_back(BatchItem{k, (int32_t)i0, (int32_t)j0, 0});
+                    P.h_edge.push_back(interior_tile(g, q, i0, j0) ? 0 : 1);
+                }
+        }
+        make_ranges(P.h_items, P.h_edge, b->grid, P.h_ranges);
     }
-    if (b->grid > kBatchMaxGrid) b->grid = kBatchMaxGrid;
-    make_ranges(b->h_items, b->h_edge, b->grid, b->h_ranges);
     cudaStream_t s = (cudaStream_t)stream;
-    if (cudaMemcpyAsync(b->d_maps, b->h_maps.data(), sizeof(BatchMaps) * n,
-                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(BatchTissue) * n,
-                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(b->d_items, b->h_items.data(), sizeof(BatchItem) * b->n_items,
-                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(b->d_ranges, b->h_ranges.data(), sizeof(int) * b->h_ranges.size(),
-                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
+    bool ok = cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(BatchTissue) * n,
+                              cudaMemcpyHostToDevice, s) == cudaSuccess;
+    for (int q = 0; q < kShapes && ok; ++q) {
+        const fk_batch::PerShape &P = b->sp[q];
+        ok = cudaMemcpyAsync(P.d_maps, P.h_maps.data(), sizeof(BatchMaps) * n,
+                             cudaMemcpyHostToDevice, s) == cudaSuccess &&
+             cudaMemcpyAsync(P.d_items, P.h_items.data(), sizeof(BatchItem) * P.n_items,
+                             cudaMemcpyHostToDevice, s) == cudaSuccess &&
+             cudaMemcpyAsync(P.d_ranges, P.h_ranges.data(), sizeof(int) * P.h_ranges.size(),
+                             cudaMemcpyHostToDevice, s) == cudaSuccess;
+    }
+    if (!ok || cudaStreamSynchronize(s) != cudaSuccess) {
         delete b;
         return FK_ERR_CUDA;
     }
@@ -244,31 +305,51 @@ int fk_batch_set_grid(fk_batch *b, int ctas) {
     if (ctas < 1 || ctas > kBatchMaxGrid) return FK_ERR_ARGUMENT;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev != b->device) return FK_ERR_CUDA;
-    std::vector<int> r;
-    make_ranges(b->h_items, b->h_edge, ctas, r);
-    // ordered after the plan's earlier work on the legacy stream; the host copy stays alive
-    if (cudaDeviceSynchronize() != cudaSuccess ||
-        cudaMemcpy(b->d_ranges, r.data(), sizeof(int) * r.size(), cudaMemcpyHostToDevice) !=
+    // ordered after the plan's earlier work; the host copies stay alive in the plan
+    if (cudaDeviceSynchronize() != cudaSuccess) return FK_ERR_CUDA;
+    for (int q = 0; q < kShapes; ++q) {
+        fk_batch::PerShape &P = b->sp[q];
+        std::vector<int> r;
+        make_ranges(P.h_items, P.h_edge, ctas, r);
+        if (cudaMemcpy(P.d_ranges, r.data(), sizeof(int) * r.size(), cudaMemcpyHostToDevice) !=
             cudaSuccess)
-        return FK_ERR_CUDA;
-    b->h_ranges.swap(r);
+            return FK_ERR_CUDA;
+        P.h_ranges.swap(r);
+    }
     b->grid = ctas;
     release_graph(b);
     return FK_OK;
 }
 
+int fk_batch_set_tile_rows(fk_batch *b, int rows) {
+    if (!b) return FK_ERR_NULL;
+    for (int q = 0; q < kShapes; ++q)
+        if (kShape[q].rows == rows) {
+            if (b->shape != q) release_graph(b);
+            b->shape = q;
+            return FK_OK;
+        }
+    return FK_ERR_ARGUMENT;
+}
+
+static cudaError_t launch_one(const fk_batch *b, int n_items, int t_offset, int parity, bool act,
+                              cudaStream_t s) {
+    const fk_batch::PerShape &P = b->sp[b->shape];
+    return kShape[b->shape].launch(b->d_tissues, P.d_maps, P.d_items, P.d_ranges, n_items, b->d_t,
+                                   t_offset, parity, act, b->status, b->grid, s);
+}
+
 static int launch_steps(fk_batch *b, int count, cudaStream_t s) {
-    for (int k = 0; k < count; ++k) {
-        cudaError_t e = launch_batch_step(b->d_tissues, b->d_maps, b->d_items, b->d_ranges,
-                                          b->n_items, b->d_t, k, k & 1, b->act, b->status,
-                                          b->grid, s);
-        if (e != cudaSuccess) return FK_ERR_CUDA;
-    }
+    const int n_items = b->sp[b->shape].n_items;
+    for (int k = 0; k < count; ++k)
+        if (launch_one(b, n_items, k, k & 1, b->act, s) != cudaSuccess) return FK_ERR_CUDA;
     return launch_add_int(b->d_t, count, s) == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
 
 static int ensure_graph(fk_batch *b, int steps) {
-    if (b->exec && b->graph_steps == steps && b->graph_grid == b->grid) return FK_OK;
+    if (b->exec && b->graph_steps == steps && b->graph_grid == b->grid &&
+        b->graph_shape == b->shape)
+        return FK_OK;
     release_graph(b);
     if (!b->capture_stream &&
         cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -290,6 +371,7 @@ static int ensure_graph(fk_batch *b, int steps) {
     b->graph = g;
     b->graph_steps = steps;
     b->graph_grid = b->grid;
+    b->graph_shape = b->shape;
     return FK_OK;
 }
 
@@ -311,10 +393,10 @@ int fk_batch_forward_euler(fk_batch *b, int64_t t0, int64_t t1, int graph_steps,
     if (graph_steps > 0) {
         const int G = (graph_steps + 1) / 2 * 2;
         if (n >= G) {
-            if (!b->exec || b->graph_steps != G || b->graph_grid != b->grid) {
-                if ((rc = launch_steps(b, 0, s))) return rc;  // configures the kernel
-                if (launch_batch_step(b->d_tissues, b->d_maps, b->d_items, b->d_ranges, 0,
-                                      b->d_t, 0, 0, b->act, b->status, b->grid, s) != cudaSuccess)
+            if (!b->exec || b->graph_steps != G || b->graph_grid != b->grid ||
+                b->graph_shape != b->shape) {
+                if ((rc = launch_steps(b, 0, s))) return rc;
+                if (launch_one(b, 0, 0, 0, b->act, s) != cudaSuccess)  // configures the kernel
                     return FK_ERR_CUDA;
                 if ((rc = ensure_graph(b, G))) return rc;
             }
@@ -363,9 +445,8 @@ int fk_batch_recompute(fk_batch *b, int64_t s, int64_t n, float *bufs, int64_t e
     if (cudaGetLastError() != cudaSuccess) return FK_ERR_CUDA;
     for (int64_t k = 1; k < n; ++k) {
         // step s+k-1 reads buffer (k-1)&1 and leaves x_{s+k} in buffer k&1
-        if (launch_batch_step(b->d_tissues, b->d_maps, b->d_items, b->d_ranges, b->n_items,
-                              b->d_t, (int)(k - 1), (int)((k - 1) & 1), false, b->status, b->grid,
-                              cs) != cudaSuccess)
+        if (launch_one(b, b->sp[b->shape].n_items, (int)(k - 1), (int)((k - 1) & 1), false, cs) !=
+            cudaSuccess)
             return FK_ERR_CUDA;
         batch_state_out_kernel<<<cgrid, 256, 0, cs>>>(b->d_tissues, (int)(k & 1), bufs + k * ns,
                                                       exp_stride, ns);

@@ -58,15 +58,6 @@ struct TileOrder {
     }
 };
 
-// After an abandoned tile n (a TMA wait ran out): the loads still in flight are those of tiles
-// n .. n+NSTAGE-2 that were issued (issued(q) for tile n+q); wait for each (bounded) so that no
-// copy lands in shared memory after the CTA has exited.  Thread 0 only.
-template <class Issued>
-__device__ __forceinline__ void drain_stages(uint64_t *bar, int n, Issued issued) {
-    for (int q = 0; q < NSTAGE - 1; ++q)
-        if (issued(q)) mbar_wait_bounded(&bar[(n + q) % NSTAGE], ((n + q) / NSTAGE) & 1);
-}
-
 // ---- the step kernel: persistent CTAs over the tiles of one tissue ------------------------
 template <bool DERIV, bool ACT, int HEUN>
 __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_constant__ StepMaps tm,
@@ -154,89 +145,6 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
     }
 }
 
-// ---- batched kernel: persistent CTAs over the tiles of many tissues ------------------------
-// CTA c processes the contiguous run items[ranges[c] .. ranges[c+1]) of the work list (the host
-// orders the list tissue by tissue and balances the runs by cost), so consecutive items mostly
-// belong to one tissue: the tissue's arguments are staged into shared memory (and its stimulus
-// mask and packed 1/dx, dt formed) only when the tissue changes, not per item.  The arithmetic
-// is the single-tissue kernel's packed path, with the launch-wide stencil coefficients of `kc`
-// as constant-bank operands and the tissue's 1/dx and dt in registers.
-template <bool ACT>
-__global__ void __launch_bounds__(NT, CTAS_PER_SM)
-    fk_batch_kernel(const BatchTissue *__restrict__ tissues, const BatchMaps *__restrict__ maps,
-                    const BatchItem *__restrict__ items, const int *__restrict__ ranges,
-                    const int *t_dev, int t_offset, int parity, int *status,
-                    const __grid_constant__ PackConsts kc) {
-    extern __shared__ unsigned char smem_raw[];
-    unsigned char *smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
-    // as fk_step_kernel: u_x / u_y double-buffered, new state stored from registers; two slots
-    // for staged tissue arguments (a new tissue is staged while slower warps may still be in
-    // pass 2 of the previous tissue's last item)
-    float *sux = reinterpret_cast<float *>(smem + NSTAGE * SMEM_STAGE_BYTES);  // [2][SUX_H][TX]
-    float *suy = sux + 2 * TX * SUX_H;                                           // [2][TY][SW]
-    TileIO io;
-    io.ov = io.ow = io.ou = nullptr;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(suy + 2 * SW * TY);            // [NSTAGE]
-    unsigned char *args = reinterpret_cast<unsigned char *>(bar + NSTAGE);       // [2] StepArgs
-
-    const int tid = threadIdx.x;
-    const int it0 = ranges[blockIdx.x], it1 = ranges[blockIdx.x + 1];
-    if (tid == 0) {
-        for (int q = 0; q < NSTAGE; ++q) mbar_init(&bar[q], 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    grid_dependency_wait();  // the previous step (and the step counter) are complete
-    grid_launch_dependents();
-    if (it0 >= it1) return;
-    const float t = (float)(*t_dev + t_offset);
-    auto issue = [&](int x, int st) {
-        const BatchItem b = items[x];
-        issue_tile(maps[b.tissue].maps[parity], stage_at(smem, st), &bar[st], b.i0, b.j0);
-    };
-    if (tid == 0)
-        for (int q = 0; q < NSTAGE - 1; ++q)
-            if (it0 + q < it1) issue(it0 + q, q);
-    int cur = -1, slot = 1;
-    unsigned active = 0;
-    PairScale ps;
-    ps.rdx = ps.dt = make_float2(0.f, 0.f);
-    BatchItem b = items[it0];
-    for (int it = it0, n = 0; it < it1; ++it, ++n) {
-        const int s = n % NSTAGE;
-        const BatchItem nb = it + 1 < it1 ? items[it + 1] : b;  // the next descriptor, early
-        if (b.tissue != cur) {  // uniform: every thread read the same item
-            slot ^= 1;
-            StepArgs *sa = reinterpret_cast<StepArgs *>(args + slot * SMEM_ARGS_BYTES);
-            stage_args(sa, &tissues[b.tissue].args[parity]);
-            __syncthreads();
-            cur = b.tissue;
-            active = 0;
-            for (int q = 0; q < sa->n_stim; ++q)
-                if (stim_active(sa->stim[q], t)) active |= 1u << q;
-            ps.rdx = make_float2(sa->rdx, sa->rdx);
-            ps.dt = make_float2(sa->dt, sa->dt);
-        }
-        const StepArgs &A = *reinterpret_cast<const StepArgs *>(args + slot * SMEM_ARGS_BYTES);
-        load_vw(A, b.i0, b.j0, io);
-        const bool ok = mbar_wait_bounded(&bar[s], (n / NSTAGE) & 1);
-        const int ahead = it + NSTAGE - 1;
-        auto refill = [&] {  // after the pass barrier: item n-1 is done, its stage is free
-            if (tid == 0 && ahead < it1) issue(ahead, (n + NSTAGE - 1) % NSTAGE);
-        };
-        float *ux_n = sux + (n & 1) * (TX * SUX_H), *uy_n = suy + (n & 1) * (SW * TY);
-        if (!process_tile<false, ACT, true, true>(A, t, stage_at(smem, s), ux_n, uy_n, io, active,
-                                                  b.i0, b.j0, NoHook{}, &kc, ps, ok, refill)) {
-            if (tid == 0) {
-                atomicOr(status, kStatusTimeout);
-                drain_stages(bar, n, [&](int q) { return it + q < it1; });
-            }
-            return;
-        }
-        b = nb;
-    }
-}
-
 __global__ void add_int_kernel(int *p, int v) { *p += v; }
 
 __global__ void batch_copyback_kernel(const BatchTissue *tissues) {
@@ -250,45 +158,6 @@ __global__ void batch_copyback_kernel(const BatchTissue *tissues) {
         for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < plane;
              k += (int64_t)gridDim.x * blockDim.x)
             out[p][k] = in[p][k];
-}
-
-cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
-                              const BatchItem *items, const int *ranges, int n_items,
-                              const int *t_dev, int t_offset, int parity, bool act, int *status,
-                              int grid, cudaStream_t stream) {
-    // function attributes belong to the context: set again whenever it changes
-    static thread_local uint64_t configured_ctx = 0;
-    if (context_changed(configured_ctx)) {
-        cudaError_t e;
-        if ((e = cudaFuncSetAttribute(fk_batch_kernel<true>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      SMEM_BATCH_BYTES)) != cudaSuccess ||
-            (e = cudaFuncSetAttribute(fk_batch_kernel<false>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      SMEM_BATCH_BYTES)) != cudaSuccess) {
-            configured_ctx = 0;
-            return e;
-        }
-    }
-    if (grid < 1 || n_items < 1) return cudaSuccess;
-    // launch-wide stencil coefficients (the per-tissue 1/dx, dt and model come from the
-    // tissues' own arguments)
-    static const PackConsts kc = make_pack_consts(Model{}, 1.0f, 1.0f);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(NT);
-    cfg.dynamicSmemBytes = SMEM_BATCH_BYTES;
-    cfg.stream = stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if (act)
-        return cudaLaunchKernelEx(&cfg, fk_batch_kernel<true>, tissues, maps, items, ranges, t_dev,
-                                  t_offset, parity, status, kc);
-    return cudaLaunchKernelEx(&cfg, fk_batch_kernel<false>, tissues, maps, items, ranges, t_dev,
-                              t_offset, parity, status, kc);
 }
 
 cudaError_t launch_add_int(int *p, int v, cudaStream_t stream) {

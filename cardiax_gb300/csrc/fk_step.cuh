@@ -6,7 +6,18 @@
 
 #include "fk_math.cuh"
 
-namespace fk {
+// The tile geometry below is compile-time.  A translation unit that builds the batched kernel
+// for another tile shape defines FK_TILE_Y / FK_TILE_X (and FK_CTAS_PER_SM) together with
+// FK_TILE_NS, the namespace that the geometry-dependent code of this header and of fk_tile.cuh
+// then lives in (the geometry-independent code of fk_math.cuh, fk_pack.cuh and fk_ptx.cuh stays
+// in namespace fk), so that the variants do not collide.
+#ifndef FK_TILE_NS
+#define FK_TILE_NS fk
+#endif
+namespace FK_TILE_NS {
+#ifdef FK_TILE_NS_VARIANT
+using namespace fk;
+#endif
 
 // Tile geometry of the step kernel.  Persistent CTAs of NT threads (two per SM) walk over
 // TY x TX tiles with a three-stage TMA ring for the haloed u and D tiles (the loads of tiles
@@ -30,7 +41,11 @@ namespace fk {
 constexpr int TX = FK_TILE_X;
 constexpr int TY = FK_TILE_Y;
 constexpr int NT = FK_THREADS;
+#ifdef FK_CTAS_PER_SM
+constexpr int CTAS_PER_SM = FK_CTAS_PER_SM;
+#else
 constexpr int CTAS_PER_SM = NT <= 256 ? 2 : 1;
+#endif
 constexpr int PASS1_UNROLL = FK_PASS1_UNROLL;
 constexpr int NTX = TX / 4;          // float4 columns
 constexpr int RPT = TY / (NT / NTX); // rows per thread in pass 2
@@ -154,4 +169,4 @@ inline int64_t flow_flag_words(int64_t H, int64_t W) {
 // tracking (FlowArgs::in[*].act_* set).
 cudaError_t launch_flow(const FlowMaps &maps, const FlowArgs &a, bool act, cudaStream_t stream);
 
-}  // namespace fk
+}  // namespace FK_TILE_NS

@@ -39,7 +39,11 @@ struct TbGeom {
     // (K = 2), a second set of the four loaded planes so that the next tile's load overlaps
     // this tile's steps
     static constexpr int SINGLE_BYTES = 7 * PLANE * 4 + 3 * OY * OX * 4;
+#ifdef FK_TB_NBUF
+    static constexpr int NBUF = FK_TB_NBUF;  // a build-time override (1: no overlap)
+#else
     static constexpr int NBUF = SINGLE_BYTES + LOAD_BYTES + 16 + 1024 + 128 <= 227 * 1024 ? 2 : 1;
+#endif
     static constexpr int BYTES = SINGLE_BYTES + (NBUF - 1) * LOAD_BYTES;
     static_assert(BX % 4 == 0 && OX % 4 == 0, "float4 rows");
     static_assert(BX <= 256 && BY <= 256, "TMA box");

@@ -25,7 +25,7 @@
 #include "fk_ptx.cuh"
 #include "fk_step.cuh"
 
-namespace fk {
+namespace FK_TILE_NS {  // see fk_step.cuh
 
 __device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
 
@@ -493,8 +493,13 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                 uxx = q_central(kc, uxr[o - 2], uxr[o - 1], uxr[o + 1], uxr[o + 2]);
                 dxD = q_central(kc, dxr[o - 2], dxr[o - 1], dxr[o + 1], dxr[o + 2]);
             } else if (k == 0 && i == 0) {  // head rows on u_x rows 0..3 and D rows 0..3
-                uxx = q_head(kc, uxr[o], uxr[o + 1], uxr[o + 2], uxr[o + 3]);
-                dxD = q_head(kc, dxr[o], dxr[o + 1], dxr[o + 2], dxr[o + 3]);
+                // row r+3 lies beyond the window when a thread owns one row (RPT == 1)
+                const Quad ux3 = o + 3 < RPT + 4 ? uxr[o + 3 < RPT + 4 ? o + 3 : 0]
+                                                 : ld_quad(sux + (r + 5) * TX + 4 * tx);
+                const Quad d3 = o + 3 < RPT + 4 ? dxr[o + 3 < RPT + 4 ? o + 3 : 0]
+                                                : ld_quad(sd + (r + 3 + HALO_D) * SW + HALO_U + 4 * tx);
+                uxx = q_head(kc, uxr[o], uxr[o + 1], uxr[o + 2], ux3);
+                dxD = q_head(kc, dxr[o], dxr[o + 1], dxr[o + 2], d3);
             } else {  // i == H-1: tail rows on rows H-4 .. H-1 (row r-3 read here when k == 0)
                 const float *xb = sux + (r + 2) * TX + 4 * tx;
                 const Quad ux3 = k >= 1 ? uxr[k >= 1 ? o - 3 : 0] : ld_quad(xb - 3 * TX);
@@ -856,6 +861,15 @@ __device__ __forceinline__ void store_tile(const StepMaps &tm, const TileIO &io,
     store_tile(&tm.ov, &tm.ow, &tm.ou, io, i0, j0);
 }
 
+// After an abandoned tile n (a TMA wait ran out): the loads still in flight are those of tiles
+// n .. n+NSTAGE-2 that were issued (issued(q) for tile n+q); wait for each (bounded) so that no
+// copy lands in shared memory after the CTA has exited.  Thread 0 only.
+template <class Issued>
+__device__ __forceinline__ void drain_stages(uint64_t *bar, int n, Issued issued) {
+    for (int q = 0; q < NSTAGE - 1; ++q)
+        if (issued(q)) mbar_wait_bounded(&bar[(n + q) % NSTAGE], ((n + q) / NSTAGE) & 1);
+}
+
 static_assert(sizeof(StepArgs) <= SMEM_ARGS_BYTES, "StepArgs does not fit its shared slot");
 
 // Copies a StepArgs into shared memory (all threads; a barrier must follow).
@@ -865,4 +879,4 @@ __device__ __forceinline__ void stage_args(StepArgs *dst, const StepArgs *src) {
     for (int k = threadIdx.x; k < (int)(sizeof(StepArgs) / 4); k += NT) d[k] = s[k];
 }
 
-}  // namespace fk
+}  // namespace FK_TILE_NS

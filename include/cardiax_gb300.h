@@ -262,8 +262,13 @@ int fk_batch_create(const fk_tissue *tissues, int n_tissues, void *workspace,
  * (rounded up to even) into a CUDA graph once per plan and replays it; 0 launches each step. */
 int fk_batch_forward_euler(fk_batch *plan, int64_t t0, int64_t t1, int graph_steps, void *stream);
 
-/* Number of persistent CTAs per launch (default: one per SM); a tuning knob. */
+/* Number of persistent CTAs per launch (default: two per SM); a tuning knob. */
 int fk_batch_set_grid(fk_batch *plan, int ctas);
+
+/* Tile geometry of the batched kernel: `rows` x 64-cell work items, rows = 32 (the default) or
+ * 16.  Both give the same bits; the autotuner picks the faster for a batch.  No counterpart in
+ * the reference. */
+int fk_batch_set_tile_rows(fk_batch *plan, int rows);
 
 int fk_batch_destroy(fk_batch *plan);
 

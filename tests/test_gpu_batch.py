@@ -42,15 +42,17 @@ def _mixed_tissues(rng, track=False):
     return out
 
 
-@pytest.mark.parametrize("graph_steps,n_steps", [(0, 37), (16, 101), (64, 64)])
-def test_batch_matches_single_tissue_bitwise(graph_steps, n_steps):
+@pytest.mark.parametrize("graph_steps,n_steps,rows", [(0, 37, 32), (16, 101, 32), (64, 64, 32),
+                                                      (0, 37, 16), (16, 101, 16)])
+def test_batch_matches_single_tissue_bitwise(graph_steps, n_steps, rows):
+    """Every tile geometry of the batched kernel (32 x 64 and 16 x 64 work items)."""
     _gpu()
     from cardiax_gb300.batch import TissueBatch
     a = _mixed_tissues(np.random.default_rng(1))
     b = _mixed_tissues(np.random.default_rng(1))
     for t in a:
         t.advance(0, n_steps)
-    batch = TissueBatch(b, graph_steps=graph_steps)
+    batch = TissueBatch(b, graph_steps=graph_steps, tile_rows=rows)
     batch.advance(0, n_steps)
     torch.cuda.synchronize()
     for x, y in zip(a, b):
@@ -85,6 +87,26 @@ def test_autotuner_restores_state_and_picks_a_candidate():
     before = [t.state.clone() for t in b]
     batch = TissueBatch(b)
     res = tune_batch(batch, trial_steps=32, candidates=(0, 16))
-    assert res["graph_steps"] in (0, 16)
+    assert res["graph_steps"] in (0, 16) and res["tile_rows"] in (32, 16)
+    assert len(res["ms_per_step"]) == 4 and batch.tile_rows == res["tile_rows"]
     for t, s in zip(b, before):
         assert torch.equal(t.state, s)
+
+
+def test_tile_geometry_switches_mid_run_and_ctas_change():
+    """Changing the tile geometry and the CTA count between calls keeps the results bitwise."""
+    _gpu()
+    from cardiax_gb300.batch import TissueBatch
+    a = _mixed_tissues(np.random.default_rng(4))
+    b = _mixed_tissues(np.random.default_rng(4))
+    for t in a:
+        t.advance(0, 90)
+    batch = TissueBatch(b, graph_steps=16)
+    batch.advance(0, 33)
+    batch.set_tile_rows(16).advance(33, 61)
+    batch.set_ctas(97).set_tile_rows(32).advance(61, 90)
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        for p, q in zip(x.view(), y.view()):
+            _same(p, q)
+    batch.close()
