@@ -96,6 +96,7 @@ _SIGNATURES = {
     "fk_batch_forward_euler": [_P, _I64, _I64, _INT, _P],
     "fk_batch_set_grid": [_P, _INT],
     "fk_batch_set_tile_rows": [_P, _INT],
+    "fk_batch_set_options": [_P, _INT, _INT],
     "fk_batch_destroy": [_P],
 }
 

@@ -1,9 +1,10 @@
 """Autotuners of the stepping configuration.
 
-``tune_batch``: for a batch, times on the batch's own tissues every combination of the tile
-geometry of the batched kernel (work items of 32 x 64 or 16 x 64 cells) and ``graph_steps``
-in {0, 16, 64, 256} (how many steps one captured CUDA graph replays) over a short run with CUDA
-events and keeps the fastest.
+``tune_batch``: for a batch, times on the batch's own tissues every combination of the batched
+kernel's tile geometry (work items of 32 x 64 or 16 x 64 cells), work order (the CTAs deal the
+work list round-robin, or each takes a contiguous run of it), arithmetic (scalar or packed
+two-cell FP32) and ``graph_steps`` (how many steps one captured CUDA graph replays) over a short
+run with CUDA events and keeps the fastest.  Every combination gives the same bits.
 
 ``tune_tissue``: for one tissue, times every way of taking its Euler steps -- the tiled step
 kernel (32 x 64-cell tiles), the strip kernel (128-column strips walked row by row), the
@@ -28,8 +29,10 @@ _TISSUE_CACHE: dict = {}
 TISSUE_CANDIDATES = (("step", 1, 0), ("step", 1, 1), ("step", 2, 0), ("step", 4, 0),
                      ("step", 8, 0), ("flow", 1, 0))
 
-GRAPH_CANDIDATES = (0, 16, 64, 256)
+GRAPH_CANDIDATES = (0, 64)
 TILE_ROW_CANDIDATES = (32, 16)
+# (interleave, packed) of the batched kernel
+OPTION_CANDIDATES = ((True, False), (False, False), (True, True), (False, True))
 
 
 def _signature(batch: TissueBatch):
@@ -37,36 +40,47 @@ def _signature(batch: TissueBatch):
     return (torch.cuda.get_device_name(batch.device), shapes)
 
 
+def _set_batch(batch: TissueBatch, cfg) -> None:
+    rows, (interleave, packed), g = cfg
+    batch.set_tile_rows(rows)
+    batch.set_options(interleave, packed)
+    batch.graph_steps = g
+
+
 def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CANDIDATES,
-               tile_rows=TILE_ROW_CANDIDATES, verbose: bool = False) -> dict:
-    """Picks the tile geometry and ``graph_steps`` for ``batch`` (set on it) and returns the
-    timings: ``{"tile_rows": r, "graph_steps": g, "ms_per_step": {(r, g): ms}}``."""
-    key = (_signature(batch), trial_steps, tuple(candidates), tuple(tile_rows))
+               tile_rows=TILE_ROW_CANDIDATES, options=OPTION_CANDIDATES,
+               verbose: bool = False) -> dict:
+    """Picks the tile geometry, work order, arithmetic and ``graph_steps`` for ``batch`` (set on
+    it) and returns ``{"tile_rows", "interleave", "packed", "graph_steps", "ms_per_step":
+    {(rows, (interleave, packed), graph_steps): ms}}``; the tissues' states are restored."""
+    key = (_signature(batch), trial_steps, tuple(candidates), tuple(tile_rows), tuple(options))
     if key in _CACHE:
         res = _CACHE[key]
-        batch.set_tile_rows(res["tile_rows"])
-        batch.graph_steps = res["graph_steps"]
+        _set_batch(batch, res["choice"])
         return res
     saved = [(t.state.clone(), None if t.activation is None else
               (t.act_first.clone(), t.act_last.clone(), t.act_count.clone()))
              for t in batch.tissues]
     timings = {}
     for rows in tile_rows:
-        batch.set_tile_rows(rows)
-        for g in candidates:
-            batch.advance(0, 2, graph_steps=0)  # warm-up
-            if g:
-                batch.advance(0, g, graph_steps=g)  # captures the graph outside the timed run
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            batch.advance(0, trial_steps, graph_steps=g)
-            e1.record()
-            torch.cuda.synchronize()
-            timings[(rows, g)] = e0.elapsed_time(e1) / trial_steps
-            if verbose:
-                print(f"autotune tile_rows={rows} graph_steps={g}: "
-                      f"{timings[(rows, g)] * 1e3:.1f} us/step")
+        for opt in options:
+            for g in candidates:
+                cfg = (rows, tuple(opt), g)
+                _set_batch(batch, cfg)
+                batch.advance(0, 2, graph_steps=0)  # warm-up
+                if g:
+                    batch.advance(0, g, graph_steps=g)  # captures the graph outside the timing
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                batch.advance(0, trial_steps, graph_steps=g)
+                e1.record()
+                torch.cuda.synchronize()
+                timings[cfg] = e0.elapsed_time(e1) / trial_steps
+                if verbose:
+                    print(f"autotune tile_rows={rows} interleave={opt[0]} packed={opt[1]} "
+                          f"graph_steps={g}: {timings[cfg] * 1e3:.1f} us/step")
     for t, (st, act) in zip(batch.tissues, saved):
         t.state.copy_(st)
         if act is not None:
@@ -74,9 +88,9 @@ def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CAND
             t.act_last.copy_(act[1])
             t.act_count.copy_(act[2])
     best = min(timings, key=timings.get)
-    batch.set_tile_rows(best[0])
-    batch.graph_steps = best[1]
-    res = {"tile_rows": best[0], "graph_steps": best[1], "ms_per_step": timings}
+    _set_batch(batch, best)
+    res = {"choice": best, "tile_rows": best[0], "interleave": best[1][0], "packed": best[1][1],
+           "graph_steps": best[2], "ms_per_step": timings}
     _CACHE[key] = res
     return res
 

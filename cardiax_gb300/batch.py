@@ -49,6 +49,7 @@ class TissueBatch:
                ctypes.byref(plan))
         self._plan = plan
         self.tile_rows = 32
+        self.interleave, self.packed = True, False
         if ctas is not None:
             self.set_ctas(ctas)
         if tile_rows != 32:
@@ -56,6 +57,13 @@ class TissueBatch:
 
     def set_ctas(self, ctas: int) -> "TissueBatch":
         N.call("fk_batch_set_grid", self._plan, int(ctas))
+        return self
+
+    def set_options(self, interleave: bool = True, packed: bool = False) -> "TissueBatch":
+        """Work order (CTAs take every G-th item, or contiguous runs of the work list) and
+        arithmetic (packed two-cell or scalar FP32) of the batched kernel; same results."""
+        N.call("fk_batch_set_options", self._plan, int(bool(interleave)), int(bool(packed)))
+        self.interleave, self.packed = bool(interleave), bool(packed)
         return self
 
     def set_tile_rows(self, rows: int) -> "TissueBatch":

@@ -23,11 +23,12 @@ using namespace fk;
 // The tile geometries the batched kernel is built for (fk_batch_rows32.cu, fk_batch_rows16.cu):
 // rows x 64 columns, u loaded with a 4-cell halo (rows + 8 rows), D with a 2-row halo.
 typedef cudaError_t (*BatchLaunchFn)(const void *, const void *, const void *, const int *, int,
-                                     const int *, int, int, bool, int *, int, cudaStream_t);
-cudaError_t fk_batch_launch_rows32(const void *, const void *, const void *, const int *, int,
-                                   const int *, int, int, bool, int *, int, cudaStream_t);
-cudaError_t fk_batch_launch_rows16(const void *, const void *, const void *, const int *, int,
-                                   const int *, int, int, bool, int *, int, cudaStream_t);
+                                     int, int, const int *, int, int, bool, int *, int,
+                                     cudaStream_t);
+cudaError_t fk_batch_launch_rows32(const void *, const void *, const void *, const int *, int, int,
+                                   int, const int *, int, int, bool, int *, int, cudaStream_t);
+cudaError_t fk_batch_launch_rows16(const void *, const void *, const void *, const int *, int, int,
+                                   int, const int *, int, int, bool, int *, int, cudaStream_t);
 namespace {
 struct TileShape {
     int rows, cols, ctas_per_sm;
@@ -41,6 +42,7 @@ const TileShape kShape[kShapes] = {{32, 64, 2, fk_batch_launch_rows32},
 struct fk_batch {
     int n = 0, grid = 0, device = -1;
     int shape = 0;  // index into kShape of the tile geometry in use
+    int interleave = 1, packed = 0;  // work order and arithmetic of the batched kernel
     BatchTissue *d_tissues = nullptr;
     int *d_t = nullptr;
     int *status = nullptr;
@@ -58,11 +60,13 @@ struct fk_batch {
     } sp[kShapes];
     // host staging (kept alive until destroy: the uploads are asynchronous)
     std::vector<BatchTissue> h_tissues;
+    std::vector<int> order;        // tissues, larger first
+    std::vector<fk_grid> grids;    // per tissue
     // captured graph
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    int graph_steps = 0, graph_grid = 0, graph_shape = 0;
+    int graph_steps = 0, graph_grid = 0, graph_shape = 0, graph_opts = 0;
 };
 
 namespace {
@@ -125,6 +129,35 @@ void make_ranges(const std::vector<BatchItem> &items, const std::vector<uint8_t>
 }
 
 bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// The work list of tile geometry `q` for the plan's work order, and the CTAs' runs of it.
+// Interleaved order: every tissue's edge tiles (the costlier clamped-halo path) first, then the
+// interior tiles, each group with the larger tissues first (CTAs take every G-th item).
+// Contiguous runs: tissue by tissue (larger first), each tissue's tiles row by row, so that a
+// CTA's run changes tissue rarely.
+void build_items(fk_batch *b, int q) {
+    fk_batch::PerShape &P = b->sp[q];
+    const TileShape &ts = kShape[q];
+    P.h_items.clear();
+    P.h_edge.clear();
+    auto add = [&](int k, int want_edge) {  // want_edge: 1 edge only, 0 interior only, -1 both
+        const fk_grid &g = b->grids[k];
+        for (int64_t i0 = 0; i0 < g.H; i0 += ts.rows)
+            for (int64_t j0 = 0; j0 < g.W; j0 += ts.cols) {
+                const int edge = interior_tile(g, q, i0, j0) ? 0 : 1;
+                if (want_edge >= 0 && edge != want_edge) continue;
+                P.h_items.push_back(BatchItem{k, (int32_t)i0, (int32_t)j0, 0});
+                P.h_edge.push_back((uint8_t)edge);
+            }
+    };
+    if (b->interleave) {
+        for (int k : b->order) add(k, 1);
+        for (int k : b->order) add(k, 0);
+    } else {
+        for (int k : b->order) add(k, -1);
+    }
+    make_ranges(P.h_items, P.h_edge, b->grid, P.h_ranges);
+}
 
 void release_graph(fk_batch *b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -196,8 +229,6 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
         P.d_ranges = reinterpret_cast<int *>(ws + L.ranges[q]);
         P.n_items = (int)n_items[q];
         P.h_maps.resize(n);
-        P.h_items.reserve(n_items[q]);
-        P.h_edge.reserve(n_items[q]);
     }
 
     // tiles of the larger tissues first: the persistent CTAs then finish together
@@ -265,21 +296,10 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
             return rc;
         }
     }
-    // work lists: tissue by tissue (larger tissues first), each tissue's tiles row by row, so
-    // that a CTA's contiguous run of items changes tissue rarely; the runs are balanced by cost
-    for (int q = 0; q < kShapes; ++q) {
-        fk_batch::PerShape &P = b->sp[q];
-        const TileShape &ts = kShape[q];
-        for (int k : order) {
-            const fk_grid &g = tissues[k].g;
-            for (int64_t i0 = 0; i0 < g.H; i0 += ts.rows)
-                for (int64_t j0 = 0; j0 < g.W; j0 += ts.cols) {
-                    P.h_items.push_back(BatchItem{k, (int32_t)i0, (int32_t)j0, 0});
-                    P.h_edge.push_back(interior_tile(g, q, i0, j0) ? 0 : 1);
-                }
-        }
-        make_ranges(P.h_items, P.h_edge, b->grid, P.h_ranges);
-    }
+    b->order = order;
+    b->grids.resize(n);
+    for (int k = 0; k < n; ++k) b->grids[k] = tissues[k].g;
+    for (int q = 0; q < kShapes; ++q) build_items(b, q);
     cudaStream_t s = (cudaStream_t)stream;
     bool ok = cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(BatchTissue) * n,
                               cudaMemcpyHostToDevice, s) == cudaSuccess;
@@ -321,6 +341,29 @@ int fk_batch_set_grid(fk_batch *b, int ctas) {
     return FK_OK;
 }
 
+int fk_batch_set_options(fk_batch *b, int interleave, int packed) {
+    if (!b) return FK_ERR_NULL;
+    const int il = interleave ? 1 : 0, pk = packed ? 1 : 0;
+    if (il != b->interleave || pk != b->packed) release_graph(b);
+    b->packed = pk;
+    if (il == b->interleave) return FK_OK;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev != b->device) return FK_ERR_CUDA;
+    b->interleave = il;
+    // the work lists change order: rebuild and upload them after the plan's earlier work
+    if (cudaDeviceSynchronize() != cudaSuccess) return FK_ERR_CUDA;
+    for (int q = 0; q < kShapes; ++q) {
+        build_items(b, q);
+        const fk_batch::PerShape &P = b->sp[q];
+        if (cudaMemcpy(P.d_items, P.h_items.data(), sizeof(BatchItem) * P.n_items,
+                       cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(P.d_ranges, P.h_ranges.data(), sizeof(int) * P.h_ranges.size(),
+                       cudaMemcpyHostToDevice) != cudaSuccess)
+            return FK_ERR_CUDA;
+    }
+    return FK_OK;
+}
+
 int fk_batch_set_tile_rows(fk_batch *b, int rows) {
     if (!b) return FK_ERR_NULL;
     for (int q = 0; q < kShapes; ++q)
@@ -335,8 +378,9 @@ int fk_batch_set_tile_rows(fk_batch *b, int rows) {
 static cudaError_t launch_one(const fk_batch *b, int n_items, int t_offset, int parity, bool act,
                               cudaStream_t s) {
     const fk_batch::PerShape &P = b->sp[b->shape];
-    return kShape[b->shape].launch(b->d_tissues, P.d_maps, P.d_items, P.d_ranges, n_items, b->d_t,
-                                   t_offset, parity, act, b->status, b->grid, s);
+    return kShape[b->shape].launch(b->d_tissues, P.d_maps, P.d_items, P.d_ranges, n_items,
+                                   b->interleave, b->packed, b->d_t, t_offset, parity, act,
+                                   b->status, b->grid, s);
 }
 
 static int launch_steps(fk_batch *b, int count, cudaStream_t s) {
@@ -347,8 +391,9 @@ static int launch_steps(fk_batch *b, int count, cudaStream_t s) {
 }
 
 static int ensure_graph(fk_batch *b, int steps) {
+    const int opts = b->interleave * 2 + b->packed;
     if (b->exec && b->graph_steps == steps && b->graph_grid == b->grid &&
-        b->graph_shape == b->shape)
+        b->graph_shape == b->shape && b->graph_opts == opts)
         return FK_OK;
     release_graph(b);
     if (!b->capture_stream &&
@@ -372,6 +417,7 @@ static int ensure_graph(fk_batch *b, int steps) {
     b->graph_steps = steps;
     b->graph_grid = b->grid;
     b->graph_shape = b->shape;
+    b->graph_opts = opts;
     return FK_OK;
 }
 
@@ -394,7 +440,7 @@ int fk_batch_forward_euler(fk_batch *b, int64_t t0, int64_t t1, int graph_steps,
         const int G = (graph_steps + 1) / 2 * 2;
         if (n >= G) {
             if (!b->exec || b->graph_steps != G || b->graph_grid != b->grid ||
-                b->graph_shape != b->shape) {
+                b->graph_shape != b->shape || b->graph_opts != b->interleave * 2 + b->packed) {
                 if ((rc = launch_steps(b, 0, s))) return rc;
                 if (launch_one(b, 0, 0, 0, b->act, s) != cudaSuccess)  // configures the kernel
                     return FK_ERR_CUDA;

@@ -11,23 +11,26 @@
 namespace FK_TILE_NS {
 
 // ---- batched kernel: persistent CTAs over the tiles of many tissues ------------------------
-// CTA c processes the contiguous run items[ranges[c] .. ranges[c+1]) of the work list (the host
-// orders the list tissue by tissue and balances the runs by cost), so consecutive items mostly
-// belong to one tissue: the tissue's arguments are staged into shared memory (and its stimulus
-// mask and packed 1/dx, dt formed) only when the tissue changes, not per item.  The arithmetic
-// is the single-tissue kernel's packed path, with the launch-wide stencil coefficients of `kc`
-// as constant-bank operands and the tissue's 1/dx and dt in registers.
-template <bool ACT>
+// Work order (uniform flag `interleave`): CTA c takes items c, c + G, c + 2G, ... (G CTAs: every
+// CTA sweeps the list at the same pace, so vertically neighbouring tiles of a tissue are loaded
+// at about the same time and share their halo rows in L2), or the contiguous run
+// items[ranges[c] .. ranges[c+1]) that the host balanced by cost (consecutive items of a CTA
+// then mostly belong to one tissue).  A tissue's arguments are staged into shared memory, and
+// its stimulus mask formed, whenever the tissue differs from the previous item's.
+// PK: the packed arithmetic of the single-tissue kernel, with the launch-wide stencil
+// coefficients of `kc` as constant-bank operands and the tissue's 1/dx and dt from its staged
+// arguments; otherwise the scalar arithmetic.  Both give the same bits.
+template <bool ACT, bool PK>
 __global__ void __launch_bounds__(NT, CTAS_PER_SM)
     fk_batch_kernel(const BatchTissue *__restrict__ tissues, const BatchMaps *__restrict__ maps,
                     const BatchItem *__restrict__ items, const int *__restrict__ ranges,
-                    const int *t_dev, int t_offset, int parity, int *status,
-                    const __grid_constant__ PackConsts kc) {
+                    int n_items, int interleave, const int *t_dev, int t_offset, int parity,
+                    int *status, const __grid_constant__ PackConsts kc) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
     // as fk_step_kernel: u_x / u_y double-buffered, new state stored from registers; two slots
     // for staged tissue arguments (a new tissue is staged while slower warps may still be in
-    // pass 2 of the previous tissue's last item)
+    // pass 2 of the previous item)
     float *sux = reinterpret_cast<float *>(smem + NSTAGE * SMEM_STAGE_BYTES);  // [2][SUX_H][TX]
     float *suy = sux + 2 * TX * SUX_H;                                           // [2][TY][SW]
     TileIO io;
@@ -36,7 +39,9 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
     unsigned char *args = reinterpret_cast<unsigned char *>(bar + NSTAGE);       // [2] StepArgs
 
     const int tid = threadIdx.x;
-    const int it0 = ranges[blockIdx.x], it1 = ranges[blockIdx.x + 1];
+    const int first = interleave ? (int)blockIdx.x : ranges[blockIdx.x];
+    const int stop = interleave ? n_items : ranges[blockIdx.x + 1];
+    const int stride = interleave ? (int)gridDim.x : 1;
     if (tid == 0) {
         for (int q = 0; q < NSTAGE; ++q) mbar_init(&bar[q], 1);
         fence_barrier_init();
@@ -44,7 +49,7 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
     __syncthreads();
     grid_dependency_wait();  // the previous step (and the step counter) are complete
     grid_launch_dependents();
-    if (it0 >= it1) return;
+    if (first >= stop) return;
     const float t = (float)(*t_dev + t_offset);
     auto issue = [&](int x, int st) {
         const BatchItem b = items[x];
@@ -52,15 +57,12 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
     };
     if (tid == 0)
         for (int q = 0; q < NSTAGE - 1; ++q)
-            if (it0 + q < it1) issue(it0 + q, q);
+            if (first + q * stride < stop) issue(first + q * stride, q);
     int cur = -1, slot = 1;
     unsigned active = 0;
-    PairScale ps;
-    ps.rdx = ps.dt = make_float2(0.f, 0.f);
-    BatchItem b = items[it0];
-    for (int it = it0, n = 0; it < it1; ++it, ++n) {
+    for (int it = first, n = 0; it < stop; it += stride, ++n) {
         const int s = n % NSTAGE;
-        const BatchItem nb = it + 1 < it1 ? items[it + 1] : b;  // the next descriptor, early
+        const BatchItem b = items[it];
         if (b.tissue != cur) {  // uniform: every thread read the same item
             slot ^= 1;
             StepArgs *sa = reinterpret_cast<StepArgs *>(args + slot * SMEM_ARGS_BYTES);
@@ -70,41 +72,48 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
             active = 0;
             for (int q = 0; q < sa->n_stim; ++q)
                 if (stim_active(sa->stim[q], t)) active |= 1u << q;
-            ps.rdx = make_float2(sa->rdx, sa->rdx);
-            ps.dt = make_float2(sa->dt, sa->dt);
         }
         const StepArgs &A = *reinterpret_cast<const StepArgs *>(args + slot * SMEM_ARGS_BYTES);
         load_vw(A, b.i0, b.j0, io);
         const bool ok = mbar_wait_bounded(&bar[s], (n / NSTAGE) & 1);
-        const int ahead = it + NSTAGE - 1;
+        const int ahead = it + (NSTAGE - 1) * stride;
         auto refill = [&] {  // after the pass barrier: item n-1 is done, its stage is free
-            if (tid == 0 && ahead < it1) issue(ahead, (n + NSTAGE - 1) % NSTAGE);
+            if (tid == 0 && ahead < stop) issue(ahead, (n + NSTAGE - 1) % NSTAGE);
         };
         float *ux_n = sux + (n & 1) * (TX * SUX_H), *uy_n = suy + (n & 1) * (SW * TY);
-        if (!process_tile<false, ACT, true, true>(A, t, stage_at(smem, s), ux_n, uy_n, io, active,
-                                                  b.i0, b.j0, NoHook{}, &kc, ps, ok, refill)) {
+        PairScale ps;
+        ps.rdx = make_float2(A.rdx, A.rdx);
+        ps.dt = make_float2(A.dt, A.dt);
+        if (!process_tile<false, ACT, PK, true>(A, t, stage_at(smem, s), ux_n, uy_n, io, active,
+                                                b.i0, b.j0, NoHook{}, PK ? &kc : nullptr, ps, ok,
+                                                refill)) {
             if (tid == 0) {
                 atomicOr(status, kStatusTimeout);
-                drain_stages(bar, n, [&](int q) { return it + q < it1; });
+                drain_stages(bar, n, it, stride, stop);
             }
             return;
         }
-        b = nb;
     }
 }
 
 cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
                               const BatchItem *items, const int *ranges, int n_items,
-                              const int *t_dev, int t_offset, int parity, bool act, int *status,
-                              int grid, cudaStream_t stream) {
+                              int interleave, int packed, const int *t_dev, int t_offset,
+                              int parity, bool act, int *status, int grid, cudaStream_t stream) {
     // function attributes belong to the context: set again whenever it changes
     static thread_local uint64_t configured_ctx = 0;
     if (context_changed(configured_ctx)) {
         cudaError_t e;
-        if ((e = cudaFuncSetAttribute(fk_batch_kernel<true>,
+        if ((e = cudaFuncSetAttribute(fk_batch_kernel<true, true>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       SMEM_BATCH_BYTES)) != cudaSuccess ||
-            (e = cudaFuncSetAttribute(fk_batch_kernel<false>,
+            (e = cudaFuncSetAttribute(fk_batch_kernel<false, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      SMEM_BATCH_BYTES)) != cudaSuccess ||
+            (e = cudaFuncSetAttribute(fk_batch_kernel<true, false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      SMEM_BATCH_BYTES)) != cudaSuccess ||
+            (e = cudaFuncSetAttribute(fk_batch_kernel<false, false>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       SMEM_BATCH_BYTES)) != cudaSuccess) {
             configured_ctx = 0;
@@ -125,11 +134,18 @@ cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    const int il = interleave ? 1 : 0;
+    if (act && packed)
+        return cudaLaunchKernelEx(&cfg, fk_batch_kernel<true, true>, tissues, maps, items, ranges,
+                                  n_items, il, t_dev, t_offset, parity, status, kc);
     if (act)
-        return cudaLaunchKernelEx(&cfg, fk_batch_kernel<true>, tissues, maps, items, ranges, t_dev,
-                                  t_offset, parity, status, kc);
-    return cudaLaunchKernelEx(&cfg, fk_batch_kernel<false>, tissues, maps, items, ranges, t_dev,
-                              t_offset, parity, status, kc);
+        return cudaLaunchKernelEx(&cfg, fk_batch_kernel<true, false>, tissues, maps, items, ranges,
+                                  n_items, il, t_dev, t_offset, parity, status, kc);
+    if (packed)
+        return cudaLaunchKernelEx(&cfg, fk_batch_kernel<false, true>, tissues, maps, items, ranges,
+                                  n_items, il, t_dev, t_offset, parity, status, kc);
+    return cudaLaunchKernelEx(&cfg, fk_batch_kernel<false, false>, tissues, maps, items, ranges,
+                              n_items, il, t_dev, t_offset, parity, status, kc);
 }
 
 }  // namespace FK_TILE_NS
@@ -138,11 +154,12 @@ cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
 // including translation unit), with the descriptor arrays passed untyped: the plan builds them
 // once (their layout does not depend on the tile geometry) and calls the variant it chose.
 cudaError_t FK_BATCH_LAUNCHER(const void *tissues, const void *maps, const void *items,
-                              const int *ranges, int n_items, const int *t_dev, int t_offset,
-                              int parity, bool act, int *status, int grid, cudaStream_t stream) {
+                              const int *ranges, int n_items, int interleave, int packed,
+                              const int *t_dev, int t_offset, int parity, bool act, int *status,
+                              int grid, cudaStream_t stream) {
     using namespace FK_TILE_NS;
     return launch_batch_step(static_cast<const BatchTissue *>(tissues),
                              static_cast<const BatchMaps *>(maps),
-                             static_cast<const BatchItem *>(items), ranges, n_items, t_dev,
-                             t_offset, parity, act, status, grid, stream);
+                             static_cast<const BatchItem *>(items), ranges, n_items, interleave,
+                             packed, t_dev, t_offset, parity, act, status, grid, stream);
 }

@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM) fk_step_kernel(const __grid_c
                                                         PairScale{k.rdx, k.dt}, ok, refill)) {
             if (tid == 0) {
                 atomicOr(a.status, kStatusTimeout);
-                drain_stages(bar, n, [&](int q) { return tile + q * (int)gridDim.x < ntiles; });
+                drain_stages(bar, n, tile, (int)gridDim.x, ntiles);
             }
             return;
         }

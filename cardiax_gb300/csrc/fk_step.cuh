@@ -131,13 +131,14 @@ struct BatchItem {
 
 constexpr int SMEM_BATCH_BYTES = SMEM_STEP_DIRECT_BYTES + SMEM_ARGS_BYTES;  // two argument slots
 
-// One Euler step of every tissue: CTA c (of `grid`) processes items[ranges[c] ..
-// ranges[c+1]); the step index is *t_dev + t_offset (so that a captured graph can be replayed
-// for successive steps).  n_items == 0 only configures the kernel (no launch).
+// One Euler step of every tissue: CTA c (of `grid`) processes items c, c + grid, ... when
+// `interleave`, else items[ranges[c] .. ranges[c+1]); `packed` selects the packed arithmetic.
+// The step index is *t_dev + t_offset (so that a captured graph can be replayed for successive
+// steps).  n_items == 0 only configures the kernel (no launch).
 cudaError_t launch_batch_step(const BatchTissue *tissues, const BatchMaps *maps,
                               const BatchItem *items, const int *ranges, int n_items,
-                              const int *t_dev, int t_offset, int parity, bool act, int *status,
-                              int grid, cudaStream_t stream);
+                              int interleave, int packed, const int *t_dev, int t_offset,
+                              int parity, bool act, int *status, int grid, cudaStream_t stream);
 // The most CTAs a batched launch may use (the size of a plan's range table).
 constexpr int kBatchMaxGrid = 4096;
 // *p += v (advances the step counter of a captured graph).

@@ -34,17 +34,9 @@ struct TbGeom {
     static constexpr int BY = OY + 8 * K + 2 * RO;  // buffer rows
     static constexpr int BX = OX + 8 * K + 2 * CO;  // buffer columns (multiple of 4)
     static constexpr int PLANE = BY * BX;           // floats per buffer
+    // shared memory: u (2), v, w, D, u_x, u_y buffers; 3 dense output tiles
+    static constexpr int BYTES = 7 * PLANE * 4 + 3 * OY * OX * 4;
     static constexpr int LOAD_BYTES = 4 * PLANE * 4;
-    // shared memory: u (2), v, w, D, u_x, u_y buffers; 3 dense output tiles; and, where it fits
-    // (K = 2), a second set of the four loaded planes so that the next tile's load overlaps
-    // this tile's steps
-    static constexpr int SINGLE_BYTES = 7 * PLANE * 4 + 3 * OY * OX * 4;
-#ifdef FK_TB_NBUF
-    static constexpr int NBUF = FK_TB_NBUF;  // a build-time override (1: no overlap)
-#else
-    static constexpr int NBUF = SINGLE_BYTES + LOAD_BYTES + 16 + 1024 + 128 <= 227 * 1024 ? 2 : 1;
-#endif
-    static constexpr int BYTES = SINGLE_BYTES + (NBUF - 1) * LOAD_BYTES;
     static_assert(BX % 4 == 0 && OX % 4 == 0, "float4 rows");
     static_assert(BX <= 256 && BY <= 256, "TMA box");
 };
@@ -238,10 +230,9 @@ __global__ void __launch_bounds__(NTH, 1)
     using G = TbGeom<K, OY, OX>;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
-    // loaded planes u, v, w, D of buffer set b at in + b * 4 PLANE; then the second u, u_x,
-    // u_y and the output tiles
-    float *in = reinterpret_cast<float *>(smem);
-    float *ub = in + G::NBUF * 4 * G::PLANE, *sux = ub + G::PLANE, *suy = sux + G::PLANE;
+    float *ua = reinterpret_cast<float *>(smem);
+    float *vb = ua + G::PLANE, *wb = vb + G::PLANE, *db = wb + G::PLANE;
+    float *ub = db + G::PLANE, *sux = ub + G::PLANE, *suy = sux + G::PLANE;
     float *ov = suy + G::PLANE, *ow = ov + OY * OX, *ou = ow + OY * OX;
     uint64_t *bar = reinterpret_cast<uint64_t *>(ou + OY * OX);
     StepArgs *sa = reinterpret_cast<StepArgs *>(bar + 2);
@@ -253,7 +244,6 @@ __global__ void __launch_bounds__(NTH, 1)
         reinterpret_cast<uint32_t *>(sa)[k] = reinterpret_cast<const uint32_t *>(&a0)[k];
     if (tid == 0) {
         mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -269,39 +259,21 @@ __global__ void __launch_bounds__(NTH, 1)
             if (stim_active(a.stim[q], (float)(t0 + s))) active_k[s] |= 1u << q;
     }
 
-    // the load of a tile into buffer set b (thread 0): u, v, w, D with the blocked halo
-    auto load = [&](int tl, int b) {
-        const int gy = (tl / ntx) * OY - 4 * K - G::RO, gx = (tl % ntx) * OX - 4 * K - G::CO;
-        float *p = in + b * 4 * G::PLANE;
-        mbar_arrive_expect_tx(&bar[b], G::LOAD_BYTES);
-        tma_load_2d(p, &tm.u, gx, gy, &bar[b]);
-        tma_load_2d(p + G::PLANE, &tm.v, gx, gy, &bar[b]);
-        tma_load_2d(p + 2 * G::PLANE, &tm.w, gx, gy, &bar[b]);
-        tma_load_2d(p + 3 * G::PLANE, &tm.d, gx, gy, &bar[b]);
-    };
-    if (tid == 0 && G::NBUF == 2 && (int)blockIdx.x < ntiles) load(blockIdx.x, 0);
     int n = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++n) {
         const int i0 = (tile / ntx) * OY, j0 = (tile % ntx) * OX;
         const int gy0 = i0 - 4 * K - G::RO, gx0 = j0 - 4 * K - G::CO;
-        const int b = G::NBUF == 2 ? (n & 1) : 0;
-        // buffer set b^1 held tile n-1, whose last reads came before the barrier that ended it
         if (tid == 0) {
-            if (G::NBUF == 1)
-                load(tile, 0);
-            else if (tile + (int)gridDim.x < ntiles)
-                load(tile + gridDim.x, b ^ 1);
+            mbar_arrive_expect_tx(&bar[0], G::LOAD_BYTES);
+            tma_load_2d(ua, &tm.u, gx0, gy0, &bar[0]);
+            tma_load_2d(vb, &tm.v, gx0, gy0, &bar[0]);
+            tma_load_2d(wb, &tm.w, gx0, gy0, &bar[0]);
+            tma_load_2d(db, &tm.d, gx0, gy0, &bar[0]);
         }
-        float *ua = in + b * 4 * G::PLANE, *vb = ua + G::PLANE, *wb = vb + G::PLANE,
-              *db = wb + G::PLANE;
-        const bool ok = mbar_wait_bounded(&bar[b], G::NBUF == 2 ? (n >> 1) & 1 : n & 1);
+        const bool ok = mbar_wait_bounded(&bar[0], n & 1);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
                 atomicOr(a0.status, kStatusTimeout);
-                // the next tile's load into the other buffer set may still be in flight: wait
-                // for it (bounded) before the CTA's shared memory goes away
-                if (G::NBUF == 2 && tile + (int)gridDim.x < ntiles)
-                    mbar_wait_bounded(&bar[b ^ 1], ((n + 1) >> 1) & 1);
                 bulk_wait_all();
             }
             return;

@@ -862,12 +862,14 @@ __device__ __forceinline__ void store_tile(const StepMaps &tm, const TileIO &io,
 }
 
 // After an abandoned tile n (a TMA wait ran out): the loads still in flight are those of tiles
-// n .. n+NSTAGE-2 that were issued (issued(q) for tile n+q); wait for each (bounded) so that no
-// copy lands in shared memory after the CTA has exited.  Thread 0 only.
-template <class Issued>
-__device__ __forceinline__ void drain_stages(uint64_t *bar, int n, Issued issued) {
+// n .. n+NSTAGE-2 that were issued -- issued(q) for tile n+q, i.e. first + q * stride < last --
+// wait for each (bounded) so that no copy lands in shared memory after the CTA has exited.
+// Thread 0 only; out of line, so that the abort path costs the step kernels no registers.
+static __device__ __noinline__ void drain_stages(uint64_t *bar, int n, int first, int stride,
+                                                 int last) {
     for (int q = 0; q < NSTAGE - 1; ++q)
-        if (issued(q)) mbar_wait_bounded(&bar[(n + q) % NSTAGE], ((n + q) / NSTAGE) & 1);
+        if (first + q * stride < last)
+            mbar_wait_bounded(&bar[(n + q) % NSTAGE], ((n + q) / NSTAGE) & 1);
 }
 
 static_assert(sizeof(StepArgs) <= SMEM_ARGS_BYTES, "StepArgs does not fit its shared slot");

@@ -270,6 +270,12 @@ int fk_batch_set_grid(fk_batch *plan, int ctas);
  * the reference. */
 int fk_batch_set_tile_rows(fk_batch *plan, int rows);
 
+/* Work order and arithmetic of the batched kernel: interleave != 0 (the default) deals the
+ * work list round-robin to the CTAs (edge tiles first), 0 gives each CTA a contiguous run of it
+ * (tissue by tissue, balanced by cost); packed != 0 uses packed two-cell FP32 instructions
+ * (default 0: scalar).  Same bits either way; tuning knobs.  No counterpart in the reference. */
+int fk_batch_set_options(fk_batch *plan, int interleave, int packed);
+
 int fk_batch_destroy(fk_batch *plan);
 
 /* ---- reverse mode ---------------------------------------------------------------------------

@@ -224,11 +224,13 @@ def rectangular_field(shape, centre, size, modulus: float, dtype=np.float32):
 
 
 # --- bilinear resize (cardiax/io.py:118-124 -> jax.image.resize "bilinear") -------------------
-def resize_weights(n_in: int, n_out: int, antialias: bool = True) -> np.ndarray:
+def resize_weights(n_in: int, n_out: int, antialias: bool = True, dtype=np.float32) -> np.ndarray:
     """(n_in, n_out) float32 weights of one resized axis: the triangle kernel max(0, 1 - |x|)
     at half-pixel centres, output p sampling s = (p + 0.5) / scale - 0.5 (scale = n_out /
-    n_in), widened by 1 / scale when downsampling with ``antialias``, normalised per output."""
-    f = np.float32
+    n_in), widened by 1 / scale when downsampling with ``antialias``, normalised per output.
+    ``dtype=np.float64`` evaluates the same formulas in double (for comparisons with other
+    implementations of the algorithm)."""
+    f = dtype
     inv = f(1.0 / (n_out / n_in))
     ks = max(inv, f(1)) if antialias else f(1)
     s = (np.arange(n_out, dtype=f) + f(0.5)) * inv - f(0.5)
@@ -240,16 +242,16 @@ def resize_weights(n_in: int, n_out: int, antialias: bool = True) -> np.ndarray:
     return np.where(valid[None, :], w, f(0)).astype(f)
 
 
-def imresize_bilinear(a: np.ndarray, size, antialias: bool = True) -> np.ndarray:
+def imresize_bilinear(a: np.ndarray, size, antialias: bool = True, dtype=np.float32) -> np.ndarray:
     """The last two axes of ``a`` resized to ``size``; an axis whose size does not change is
-    left as it is."""
-    out = np.asarray(a, dtype=np.float32)
+    left as it is.  Float32 like JAX (``dtype=np.float64``: the same in double)."""
+    out = np.asarray(a, dtype=dtype)
     H, W = out.shape[-2:]
     if int(size[0]) != H:
-        out = np.einsum("...hw,ho->...ow", out, resize_weights(H, int(size[0]), antialias))
+        out = np.einsum("...hw,ho->...ow", out, resize_weights(H, int(size[0]), antialias, dtype))
     if int(size[1]) != W:
-        out = np.einsum("...hw,wo->...ho", out, resize_weights(W, int(size[1]), antialias))
-    return out.astype(np.float32)
+        out = np.einsum("...hw,wo->...ho", out, resize_weights(W, int(size[1]), antialias, dtype))
+    return out.astype(dtype)
 
 
 # --- rotated fields (cardiax/stimulus.py:109-140 -> scipy.ndimage.rotate) ----------------------

@@ -42,10 +42,13 @@ def _mixed_tissues(rng, track=False):
     return out
 
 
-@pytest.mark.parametrize("graph_steps,n_steps,rows", [(0, 37, 32), (16, 101, 32), (64, 64, 32),
-                                                      (0, 37, 16), (16, 101, 16)])
-def test_batch_matches_single_tissue_bitwise(graph_steps, n_steps, rows):
-    """Every tile geometry of the batched kernel (32 x 64 and 16 x 64 work items)."""
+@pytest.mark.parametrize("graph_steps,n_steps,rows,interleave,packed", [
+    (0, 37, 32, True, False), (16, 101, 32, True, False), (64, 64, 32, True, False),
+    (0, 37, 16, True, False), (16, 101, 16, True, False), (0, 37, 32, False, False),
+    (16, 101, 32, False, True), (0, 37, 16, False, True), (16, 64, 16, True, True)])
+def test_batch_matches_single_tissue_bitwise(graph_steps, n_steps, rows, interleave, packed):
+    """Every tile geometry (32 x 64, 16 x 64 work items), work order and arithmetic of the
+    batched kernel."""
     _gpu()
     from cardiax_gb300.batch import TissueBatch
     a = _mixed_tissues(np.random.default_rng(1))
@@ -53,6 +56,7 @@ def test_batch_matches_single_tissue_bitwise(graph_steps, n_steps, rows):
     for t in a:
         t.advance(0, n_steps)
     batch = TissueBatch(b, graph_steps=graph_steps, tile_rows=rows)
+    batch.set_options(interleave, packed)
     batch.advance(0, n_steps)
     torch.cuda.synchronize()
     for x, y in zip(a, b):
@@ -88,7 +92,8 @@ def test_autotuner_restores_state_and_picks_a_candidate():
     batch = TissueBatch(b)
     res = tune_batch(batch, trial_steps=32, candidates=(0, 16))
     assert res["graph_steps"] in (0, 16) and res["tile_rows"] in (32, 16)
-    assert len(res["ms_per_step"]) == 4 and batch.tile_rows == res["tile_rows"]
+    assert len(res["ms_per_step"]) == 16 and batch.tile_rows == res["tile_rows"]
+    assert (batch.interleave, batch.packed) == (res["interleave"], res["packed"])
     for t, s in zip(b, before):
         assert torch.equal(t.state, s)
 
@@ -103,8 +108,8 @@ def test_tile_geometry_switches_mid_run_and_ctas_change():
         t.advance(0, 90)
     batch = TissueBatch(b, graph_steps=16)
     batch.advance(0, 33)
-    batch.set_tile_rows(16).advance(33, 61)
-    batch.set_ctas(97).set_tile_rows(32).advance(61, 90)
+    batch.set_tile_rows(16).set_options(False, True).advance(33, 61)
+    batch.set_ctas(97).set_tile_rows(32).set_options(True, True).advance(61, 90)
     torch.cuda.synchronize()
     for x, y in zip(a, b):
         for p, q in zip(x.view(), y.view()):

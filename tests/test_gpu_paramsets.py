@@ -6,7 +6,8 @@ Bars (float32): max|du| <= 1e-4 at every checkpoint of 1000 steps against the re
 float32 run; against its float64 (x64) run the GPU must be as close as the reference's own
 float32 run is, within the same 1e-4 (under sets 1A/4A/5 the float32 parameters alone put the
 reference's float32 run 1.4e-4 .. 5.8e-4 away from its float64 run at 1000 steps).  On the
-large batched sample v and w meet the 1e-4 bar in all but 1e-5 of the cells: a cell whose u
+large batched sample v and w meet the 1e-4 bar in all but 1e-5 of the cells (or 4 cells on a
+small tissue): a cell whose u
 lands within an ulp of the gate threshold V_c flips its Heaviside gate a step earlier or later
 than the oracle's, which moves its v or w by up to ~1e-2 while u stays within the bar.
 """
@@ -103,7 +104,8 @@ def test_batched_workload_sample_vs_c_oracle():
             if var == "u":
                 worst = max(worst, e)
                 assert e <= TOL_U, (shape, P[:2], var, e)
-            else:  # gate flips at u ~ V_c: a few cells, never far
-                assert float((d > TOL_U).mean()) <= 1e-5 and e <= 1e-2, (shape, P[:2], var, e)
+            else:  # gate flips at u ~ V_c: a few cells (1e-5 of them, or 4), never far
+                n_off = int((d > TOL_U).sum())
+                assert n_off <= max(4, 1e-5 * d.size) and e <= 1e-2, (shape, P[:2], var, e, n_off)
     batch.close()
     print(f"batched sample (16 tissues, 1000 steps): max|du| vs the C oracle {worst:.3g}")
