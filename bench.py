@@ -164,11 +164,12 @@ def run_batched(steps: int, reps: int, dev):
     return {"tissues": len(tissues), "cells": cells, "euler_steps": steps,
             "gcups": gcups, "plain_loop_gcups": cells * steps / tl / 1e9,
             "speedup_vs_plain_loop": tl / tb, "frac": gcups * BYTES_PER_UPDATE / peak,
-            "tile_rows": tune["tile_rows"], "interleave": tune["interleave"],
-            "packed": tune["packed"], "graph_steps": tune["graph_steps"],
+            "depth": tune["depth"], "tile_rows": tune["tile_rows"],
+            "interleave": tune["interleave"], "packed": tune["packed"],
+            "graph_steps": tune["graph_steps"],
             "autotune_ms_per_step": {
-                f"rows{k[0]}_{'rr' if k[1][0] else 'runs'}_{'pk' if k[1][1] else 'sc'}_g{k[2]}": v
-                for k, v in tune["ms_per_step"].items()},
+                f"d{k[0]}_rows{k[1]}_{'rr' if k[2][0] else 'runs'}_{'pk' if k[2][1] else 'sc'}"
+                f"_g{k[3]}": v for k, v in tune["ms_per_step"].items()},
             "workload": "256 tissues, sizes {64^2,128^2,256^2,512^2,256x1024}, sets "
                         "{1A,3,4A,5}, scar D (factor U[0,0.1], floor 1e-4, blur 2), plane or "
                         "10x10 point stimulus, start U[0,5000], period U[15000,40000] steps"}

@@ -97,6 +97,7 @@ _SIGNATURES = {
     "fk_batch_set_grid": [_P, _INT],
     "fk_batch_set_tile_rows": [_P, _INT],
     "fk_batch_set_options": [_P, _INT, _INT],
+    "fk_batch_set_depth": [_P, _INT],
     "fk_batch_destroy": [_P],
 }
 

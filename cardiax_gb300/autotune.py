@@ -1,10 +1,12 @@
 """Autotuners of the stepping configuration.
 
-``tune_batch``: for a batch, times on the batch's own tissues every combination of the batched
-kernel's tile geometry (work items of 32 x 64 or 16 x 64 cells), work order (the CTAs deal the
-work list round-robin, or each takes a contiguous run of it), arithmetic (scalar or packed
-two-cell FP32) and ``graph_steps`` (how many steps one captured CUDA graph replays) over a short
-run with CUDA events and keeps the fastest.  Every combination gives the same bits.
+``tune_batch``: for a batch, times on the batch's own tissues every combination of the
+temporal-block depth (one Euler step per launch, or two: the blocked kernel), and at depth 1
+the batched kernel's tile geometry (work items of 32 x 64 or 16 x 64 cells), work order (the
+CTAs deal the work list round-robin, or each takes a contiguous run of it) and arithmetic
+(scalar or packed two-cell FP32), each with every ``graph_steps`` (how many steps one captured
+CUDA graph replays), over a short run with CUDA events, and keeps the fastest.  Every
+combination gives the same bits.
 
 ``tune_tissue``: for one tissue, times every way of taking its Euler steps -- the tiled step
 kernel (32 x 64-cell tiles), the strip kernel (128-column strips walked row by row), the
@@ -40,8 +42,12 @@ def _signature(batch: TissueBatch):
     return (torch.cuda.get_device_name(batch.device), shapes)
 
 
+DEPTH_CANDIDATES = (1, 2)
+
+
 def _set_batch(batch: TissueBatch, cfg) -> None:
-    rows, (interleave, packed), g = cfg
+    depth, rows, (interleave, packed), g = cfg
+    batch.set_depth(depth)
     batch.set_tile_rows(rows)
     batch.set_options(interleave, packed)
     batch.graph_steps = g
@@ -49,11 +55,15 @@ def _set_batch(batch: TissueBatch, cfg) -> None:
 
 def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CANDIDATES,
                tile_rows=TILE_ROW_CANDIDATES, options=OPTION_CANDIDATES,
-               verbose: bool = False) -> dict:
-    """Picks the tile geometry, work order, arithmetic and ``graph_steps`` for ``batch`` (set on
-    it) and returns ``{"tile_rows", "interleave", "packed", "graph_steps", "ms_per_step":
-    {(rows, (interleave, packed), graph_steps): ms}}``; the tissues' states are restored."""
-    key = (_signature(batch), trial_steps, tuple(candidates), tuple(tile_rows), tuple(options))
+               depths=DEPTH_CANDIDATES, verbose: bool = False) -> dict:
+    """Picks the depth, tile geometry, work order, arithmetic and ``graph_steps`` for ``batch``
+    (set on it) and returns ``{"depth", "tile_rows", "interleave", "packed", "graph_steps",
+    "ms_per_step": {(depth, rows, (interleave, packed), graph_steps): ms}}``; the tissues'
+    states are restored.  Depth 2 is tried only when the batch can be blocked; its tiles are
+    32 x 64 and it takes no work-order or arithmetic options."""
+    depths = tuple(d for d in depths if d == 1 or batch.can_block())
+    key = (_signature(batch), trial_steps, tuple(candidates), tuple(tile_rows), tuple(options),
+           depths)
     if key in _CACHE:
         res = _CACHE[key]
         _set_batch(batch, res["choice"])
@@ -62,25 +72,26 @@ def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CAND
               (t.act_first.clone(), t.act_last.clone(), t.act_count.clone()))
              for t in batch.tissues]
     timings = {}
-    for rows in tile_rows:
-        for opt in options:
-            for g in candidates:
-                cfg = (rows, tuple(opt), g)
-                _set_batch(batch, cfg)
-                batch.advance(0, 2, graph_steps=0)  # warm-up
-                if g:
-                    batch.advance(0, g, graph_steps=g)  # captures the graph outside the timing
-                torch.cuda.synchronize()
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record()
-                batch.advance(0, trial_steps, graph_steps=g)
-                e1.record()
-                torch.cuda.synchronize()
-                timings[cfg] = e0.elapsed_time(e1) / trial_steps
-                if verbose:
-                    print(f"autotune tile_rows={rows} interleave={opt[0]} packed={opt[1]} "
-                          f"graph_steps={g}: {timings[cfg] * 1e3:.1f} us/step")
+    configs = [(1, rows, tuple(opt), g) for rows in tile_rows for opt in options
+               for g in candidates]
+    configs += [(d, 32, (True, False), g) for d in depths if d != 1 for g in candidates]
+    for cfg in configs:
+        depth, rows, opt, g = cfg
+        _set_batch(batch, cfg)
+        batch.advance(0, 2, graph_steps=0)  # warm-up
+        if g:
+            batch.advance(0, g, graph_steps=g)  # captures the graph outside the timing
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        batch.advance(0, trial_steps, graph_steps=g)
+        e1.record()
+        torch.cuda.synchronize()
+        timings[cfg] = e0.elapsed_time(e1) / trial_steps
+        if verbose:
+            print(f"autotune depth={depth} tile_rows={rows} interleave={opt[0]} "
+                  f"packed={opt[1]} graph_steps={g}: {timings[cfg] * 1e3:.1f} us/step")
     for t, (st, act) in zip(batch.tissues, saved):
         t.state.copy_(st)
         if act is not None:
@@ -89,8 +100,8 @@ def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CAND
             t.act_count.copy_(act[2])
     best = min(timings, key=timings.get)
     _set_batch(batch, best)
-    res = {"choice": best, "tile_rows": best[0], "interleave": best[1][0], "packed": best[1][1],
-           "graph_steps": best[2], "ms_per_step": timings}
+    res = {"choice": best, "depth": best[0], "tile_rows": best[1], "interleave": best[2][0],
+           "packed": best[2][1], "graph_steps": best[3], "ms_per_step": timings}
     _CACHE[key] = res
     return res
 

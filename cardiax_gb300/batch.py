@@ -50,6 +50,7 @@ class TissueBatch:
         self._plan = plan
         self.tile_rows = 32
         self.interleave, self.packed = True, False
+        self.depth = 1
         if ctas is not None:
             self.set_ctas(ctas)
         if tile_rows != 32:
@@ -65,6 +66,20 @@ class TissueBatch:
         N.call("fk_batch_set_options", self._plan, int(bool(interleave)), int(bool(packed)))
         self.interleave, self.packed = bool(interleave), bool(packed)
         return self
+
+    def set_depth(self, depth: int) -> "TissueBatch":
+        """Euler steps per launch: 1, or 2 (the temporally blocked kernel: each 32 x 64 tile
+        advanced two steps between one load and one store).  Depth 2 needs every tissue's last
+        tile row and column to hold more than one cell and no activation tracking (raises
+        FkError otherwise); the results do not change."""
+        N.call("fk_batch_set_depth", self._plan, int(depth))
+        self.depth = int(depth)
+        return self
+
+    def can_block(self) -> bool:
+        """Whether depth 2 is available for this batch."""
+        return (all(t.activation is None for t in self.tissues) and
+                all(t.H % 32 != 1 and t.W % 64 != 1 for t in self.tissues))
 
     def set_tile_rows(self, rows: int) -> "TissueBatch":
         """Work items of ``rows`` x 64 cells (32 or 16); the results do not change."""

@@ -17,6 +17,7 @@
 #include "../../include/cardiax_gb300.h"
 #include "fk_capi_internal.h"
 #include "fk_step.cuh"
+#include "fk_tb.cuh"
 
 using namespace fk;
 
@@ -43,6 +44,11 @@ struct fk_batch {
     int n = 0, grid = 0, device = -1;
     int shape = 0;  // index into kShape of the tile geometry in use
     int interleave = 1, packed = 0;  // work order and arithmetic of the batched kernel
+    int depth = 1;                   // Euler steps per launch: 1, or 2 (blocked kernel)
+    bool tb_ok = false;              // every tissue can be blocked (and no activation tracking)
+    BatchTbMaps *d_tbmaps = nullptr;
+    int grid_tb = 0;                 // CTAs of the blocked kernel (one per SM)
+    std::vector<BatchTbMaps> h_tbmaps;
     BatchTissue *d_tissues = nullptr;
     int *d_t = nullptr;
     int *status = nullptr;
@@ -66,7 +72,7 @@ struct fk_batch {
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    int graph_steps = 0, graph_grid = 0, graph_shape = 0, graph_opts = 0;
+    int graph_steps = 0, graph_grid = 0, graph_shape = 0, graph_opts = 0, graph_depth = 1;
 };
 
 namespace {
@@ -80,7 +86,7 @@ int64_t tiles_of(const fk_grid &g, int shape) {
 }
 
 struct Layout {
-    size_t maps[kShapes], tissues, items[kShapes], ranges[kShapes], t, total;
+    size_t maps[kShapes], tbmaps, tissues, items[kShapes], ranges[kShapes], t, total;
 };
 
 Layout layout(int n, const int64_t *n_items) {
@@ -90,6 +96,8 @@ Layout layout(int n, const int64_t *n_items) {
         L.maps[k] = at;
         at = align_up(at + sizeof(BatchMaps) * n);
     }
+    L.tbmaps = at;
+    at = align_up(at + sizeof(BatchTbMaps) * n);
     L.tissues = at;
     at = align_up(at + sizeof(BatchTissue) * n);
     for (int k = 0; k < kShapes; ++k) {
@@ -217,9 +225,14 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
     int n_sm = 0;
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, b->device);
     b->grid = n_sm > 0 ? n_sm * kShape[0].ctas_per_sm : 1;
+    b->grid_tb = n_sm > 0 ? n_sm : 1;
     if (b->grid > kBatchMaxGrid) b->grid = kBatchMaxGrid;
     char *ws = static_cast<char *>(workspace);
     b->d_tissues = reinterpret_cast<BatchTissue *>(ws + L.tissues);
+    b->d_tbmaps = reinterpret_cast<BatchTbMaps *>(ws + L.tbmaps);
+    b->h_tbmaps.resize(n);
+    b->tb_ok = !any_act;
+    for (int k = 0; k < n; ++k) b->tb_ok &= tb_batchable(tissues[k].g.H, tissues[k].g.W);
     b->d_t = reinterpret_cast<int *>(ws + L.t);
     b->h_tissues.resize(n);
     for (int q = 0; q < kShapes; ++q) {
@@ -263,6 +276,25 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
                     break;
             }
         }
+        // the blocked kernel's maps (haloed boxes of the loaded planes, output-tile boxes)
+        if (!rc && b->tb_ok) {
+            int bw = 0, bh = 0, ow = 0, oh = 0;
+            tb_box(kBatchTbDepth, &bw, &bh, &ow, &oh);
+            const fk_grid &g = t.g;
+            for (int p = 0; p < 2 && !rc; ++p) {
+                const float *in = p ? t.scratch : t.state;
+                float *o = p ? t.state : t.scratch;
+                TbMaps &tm = b->h_tbmaps[k].maps[p];
+                if ((rc = make_plane_map(&tm.d, t.D, g.H, g.W, g.pitch, bw, bh)) ||
+                    (rc = make_plane_map(&tm.v, in, g.H, g.W, g.pitch, bw, bh)) ||
+                    (rc = make_plane_map(&tm.w, in + plane, g.H, g.W, g.pitch, bw, bh)) ||
+                    (rc = make_plane_map(&tm.u, in + 2 * plane, g.H, g.W, g.pitch, bw, bh)) ||
+                    (rc = make_plane_map(&tm.ov, o, g.H, g.W, g.pitch, ow, oh)) ||
+                    (rc = make_plane_map(&tm.ow, o + plane, g.H, g.W, g.pitch, ow, oh)) ||
+                    (rc = make_plane_map(&tm.ou, o + 2 * plane, g.H, g.W, g.pitch, ow, oh)))
+                    break;
+            }
+        }
         for (int p = 0; p < 2 && !rc; ++p) {
             const float *in = p ? t.scratch : t.state;
             float *o = p ? t.state : t.scratch;
@@ -303,6 +335,9 @@ int fk_batch_create(const fk_tissue *tissues, int n, void *workspace, size_t byt
     cudaStream_t s = (cudaStream_t)stream;
     bool ok = cudaMemcpyAsync(b->d_tissues, b->h_tissues.data(), sizeof(BatchTissue) * n,
                               cudaMemcpyHostToDevice, s) == cudaSuccess;
+    if (ok && b->tb_ok)
+        ok = cudaMemcpyAsync(b->d_tbmaps, b->h_tbmaps.data(), sizeof(BatchTbMaps) * n,
+                             cudaMemcpyHostToDevice, s) == cudaSuccess;
     for (int q = 0; q < kShapes && ok; ++q) {
         const fk_batch::PerShape &P = b->sp[q];
         ok = cudaMemcpyAsync(P.d_maps, P.h_maps.data(), sizeof(BatchMaps) * n,
@@ -364,6 +399,15 @@ int fk_batch_set_options(fk_batch *b, int interleave, int packed) {
     return FK_OK;
 }
 
+int fk_batch_set_depth(fk_batch *b, int depth) {
+    if (!b) return FK_ERR_NULL;
+    if (depth != 1 && depth != kBatchTbDepth) return FK_ERR_ARGUMENT;
+    if (depth != 1 && !b->tb_ok) return FK_ERR_ARGUMENT;
+    if (depth != b->depth) release_graph(b);
+    b->depth = depth;
+    return FK_OK;
+}
+
 int fk_batch_set_tile_rows(fk_batch *b, int rows) {
     if (!b) return FK_ERR_NULL;
     for (int q = 0; q < kShapes; ++q)
@@ -383,17 +427,35 @@ static cudaError_t launch_one(const fk_batch *b, int n_items, int t_offset, int 
                                    b->status, b->grid, s);
 }
 
+// Buffer flips of `count` steps (each launch reads one buffer and writes the other): one per
+// step at depth 1; at depth 2 one per pair of steps plus one for an odd last step.
+static int64_t flips(const fk_batch *b, int64_t count) {
+    return b->depth == 1 ? count : count / 2 + (count & 1);
+}
+
 static int launch_steps(fk_batch *b, int count, cudaStream_t s) {
-    const int n_items = b->sp[b->shape].n_items;
-    for (int k = 0; k < count; ++k)
-        if (launch_one(b, n_items, k, k & 1, b->act, s) != cudaSuccess) return FK_ERR_CUDA;
+    if (b->depth == 1) {
+        const int n_items = b->sp[b->shape].n_items;
+        for (int k = 0; k < count; ++k)
+            if (launch_one(b, n_items, k, k & 1, b->act, s) != cudaSuccess) return FK_ERR_CUDA;
+    } else {  // two steps per launch of the blocked kernel (32 x 64 work items), then the odd one
+        const fk_batch::PerShape &P = b->sp[0];
+        int k = 0, f = 0;
+        for (; k + 2 <= count; k += 2, ++f)
+            if (launch_batch_tb(b->d_tissues, b->d_tbmaps, P.d_items, P.n_items, b->d_t, k, f & 1,
+                                b->status, b->grid_tb, s) != cudaSuccess)
+                return FK_ERR_CUDA;
+        if (k < count &&
+            launch_one(b, b->sp[b->shape].n_items, k, f & 1, b->act, s) != cudaSuccess)
+            return FK_ERR_CUDA;
+    }
     return launch_add_int(b->d_t, count, s) == cudaSuccess ? FK_OK : FK_ERR_CUDA;
 }
 
 static int ensure_graph(fk_batch *b, int steps) {
     const int opts = b->interleave * 2 + b->packed;
     if (b->exec && b->graph_steps == steps && b->graph_grid == b->grid &&
-        b->graph_shape == b->shape && b->graph_opts == opts)
+        b->graph_shape == b->shape && b->graph_opts == opts && b->graph_depth == b->depth)
         return FK_OK;
     release_graph(b);
     if (!b->capture_stream &&
@@ -418,6 +480,7 @@ static int ensure_graph(fk_batch *b, int steps) {
     b->graph_grid = b->grid;
     b->graph_shape = b->shape;
     b->graph_opts = opts;
+    b->graph_depth = b->depth;
     return FK_OK;
 }
 
@@ -437,12 +500,20 @@ int fk_batch_forward_euler(fk_batch *b, int64_t t0, int64_t t1, int graph_steps,
     // the smem attribute must be set outside any capture: one plain (empty-range) call does it
     int rc;
     if (graph_steps > 0) {
-        const int G = (graph_steps + 1) / 2 * 2;
+        // a replay must flip the buffers an even number of times: G steps, G even (depth 1) or
+        // a multiple of 4 (depth 2: G / 2 launches)
+        const int q = b->depth == 1 ? 2 : 4;
+        const int G = (graph_steps + q - 1) / q * q;
         if (n >= G) {
             if (!b->exec || b->graph_steps != G || b->graph_grid != b->grid ||
-                b->graph_shape != b->shape || b->graph_opts != b->interleave * 2 + b->packed) {
+                b->graph_shape != b->shape || b->graph_opts != b->interleave * 2 + b->packed ||
+                b->graph_depth != b->depth) {
                 if ((rc = launch_steps(b, 0, s))) return rc;
                 if (launch_one(b, 0, 0, 0, b->act, s) != cudaSuccess)  // configures the kernel
+                    return FK_ERR_CUDA;
+                if (b->depth != 1 &&
+                    launch_batch_tb(b->d_tissues, b->d_tbmaps, b->sp[0].d_items, 0, b->d_t, 0, 0,
+                                    b->status, b->grid_tb, s) != cudaSuccess)
                     return FK_ERR_CUDA;
                 if ((rc = ensure_graph(b, G))) return rc;
             }
@@ -452,7 +523,7 @@ int fk_batch_forward_euler(fk_batch *b, int64_t t0, int64_t t1, int graph_steps,
         }
     }
     if ((rc = launch_steps(b, (int)n, s))) return rc;
-    if ((t1 - t0) & 1) {
+    if (flips(b, n) & 1) {  // the replayed graphs flipped an even number of times
         if (launch_batch_copyback(b->d_tissues, b->n, s) != cudaSuccess) return FK_ERR_CUDA;
     }
     return FK_OK;

@@ -319,6 +319,111 @@ __global__ void __launch_bounds__(NTH, 1)
     if (tid == 0) bulk_wait_all();
 }
 
+// Batched blocked stepping (depth K, OY x OX output tiles): the tile loop of fk_tb_kernel over
+// the items of many tissues, each tissue's arguments staged into shared memory whenever the
+// tissue changes (all threads have finished the previous item by then: every item ends with a
+// CTA barrier), the TMA maps read from the device descriptors of the item's tissue.
+template <int K, int OY, int OX, int NTH>
+__global__ void __launch_bounds__(NTH, 1)
+    fk_batch_tb_kernel(const BatchTissue *__restrict__ tissues,
+                       const BatchTbMaps *__restrict__ maps, const BatchItem *__restrict__ items,
+                       int n_items, const int *t_dev, int t_offset, int parity, int *status) {
+    using G = TbGeom<K, OY, OX>;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
+    float *ua = reinterpret_cast<float *>(smem);
+    float *vb = ua + G::PLANE, *wb = vb + G::PLANE, *db = wb + G::PLANE;
+    float *ub = db + G::PLANE, *sux = ub + G::PLANE, *suy = sux + G::PLANE;
+    float *ov = suy + G::PLANE, *ow = ov + OY * OX, *ou = ow + OY * OX;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(ou + OY * OX);
+    StepArgs *sa = reinterpret_cast<StepArgs *>(bar + 2);
+
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    grid_dependency_wait();  // the previous launch (and the step counter) are complete
+    grid_launch_dependents();
+    const int64_t t0 = (int64_t)(*t_dev) + t_offset;
+    int cur = -1;
+    unsigned active_k[K];
+#pragma unroll
+    for (int s = 0; s < K; ++s) active_k[s] = 0;
+    int n = 0;
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x, ++n) {
+        const BatchItem bi = items[it];
+        if (bi.tissue != cur) {  // uniform
+            stage_args(sa, &tissues[bi.tissue].args[parity]);
+            __syncthreads();
+            cur = bi.tissue;
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                active_k[s] = 0;
+                for (int q = 0; q < sa->n_stim; ++q)
+                    if (stim_active(sa->stim[q], (float)(t0 + s))) active_k[s] |= 1u << q;
+            }
+        }
+        const StepArgs &a = *sa;
+        const TbMaps &tm = maps[bi.tissue].maps[parity];
+        const int H = a.H, W = a.W, i0 = bi.i0, j0 = bi.j0;
+        const int gy0 = i0 - 4 * K - G::RO, gx0 = j0 - 4 * K - G::CO;
+        if (tid == 0) {
+            mbar_arrive_expect_tx(&bar[0], G::LOAD_BYTES);
+            tma_load_2d(ua, &tm.u, gx0, gy0, &bar[0]);
+            tma_load_2d(vb, &tm.v, gx0, gy0, &bar[0]);
+            tma_load_2d(wb, &tm.w, gx0, gy0, &bar[0]);
+            tma_load_2d(db, &tm.d, gx0, gy0, &bar[0]);
+        }
+        const bool ok = mbar_wait_bounded(&bar[0], n & 1);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(status, kStatusTimeout);
+                bulk_wait_all();
+            }
+            return;
+        }
+        const bool edge = !(gy0 - 4 >= 0 && gy0 + G::BY + 4 <= H && gx0 - 4 >= 0 &&
+                            gx0 + G::BX + 4 <= W);
+        if (edge) {
+            tb_clamp<G::BY, G::BX, NTH>(ua, gy0, gx0, H, W);
+            tb_clamp<G::BY, G::BX, NTH>(db, gy0, gx0, H, W);
+            __syncthreads();
+        }
+        float *cu = ua, *nx = ub;
+#pragma unroll 1
+        for (int s = 0; s < K; ++s) {
+            const bool last = s == K - 1;
+            const float t = (float)(t0 + s);
+            if (edge)
+                tb_step<K, OY, OX, NTH, true>(a, t, active_k[s], s, last, cu, nx, vb, wb, db, sux,
+                                              suy, ov, ow, ou, gy0, gx0);
+            else
+                tb_step<K, OY, OX, NTH, false>(a, t, active_k[s], s, last, cu, nx, vb, wb, db,
+                                               sux, suy, ov, ow, ou, gy0, gx0);
+            if (!last) {
+                float *tmp = cu;
+                cu = nx;
+                nx = tmp;
+                if (edge) {
+                    tb_clamp<G::BY, G::BX, NTH>(cu, gy0, gx0, H, W);
+                    __syncthreads();
+                }
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tma_store_2d(&tm.ov, ov, j0, i0);
+            tma_store_2d(&tm.ow, ow, j0, i0);
+            tma_store_2d(&tm.ou, ou, j0, i0);
+            bulk_commit();
+        }
+    }
+    if (tid == 0) bulk_wait_all();
+}
+
 namespace {
 
 template <int K, int OY, int OX>
@@ -365,6 +470,37 @@ void tb_box(int depth, int *box_w, int *box_h, int *out_w, int *out_h) {
         case 8: *box_w = TbGeom<8, 16, 16>::BX; *box_h = TbGeom<8, 16, 16>::BY; *out_w = 16; *out_h = 16; break;
         default: *box_w = *box_h = *out_w = *out_h = 0;
     }
+}
+
+cudaError_t launch_batch_tb(const BatchTissue *tissues, const BatchTbMaps *maps,
+                            const BatchItem *items, int n_items, const int *t_dev, int t_offset,
+                            int parity, int *status, int grid, cudaStream_t stream) {
+    constexpr int K = kBatchTbDepth, OY = kBatchTbRows, OX = kBatchTbCols, NTH = kTbThreads;
+    using G = TbGeom<K, OY, OX>;
+    constexpr int SMEM = G::BYTES + 16 + SMEM_ARGS_BYTES + 128;
+    static_assert(SMEM <= 227 * 1024, "blocked tile does not fit in shared memory");
+    static thread_local uint64_t configured_ctx = 0;  // attributes belong to the context
+    if (context_changed(configured_ctx)) {
+        cudaError_t e = cudaFuncSetAttribute(fk_batch_tb_kernel<K, OY, OX, NTH>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+        if (e != cudaSuccess) {
+            configured_ctx = 0;
+            return e;
+        }
+    }
+    if (grid < 1 || n_items < 1) return cudaSuccess;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(NTH);
+    cfg.dynamicSmemBytes = SMEM;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, fk_batch_tb_kernel<K, OY, OX, NTH>, tissues, maps, items,
+                              n_items, t_dev, t_offset, parity, status);
 }
 
 cudaError_t launch_tb(int depth, const TbMaps &maps, const StepArgs &a, int64_t t0,

@@ -276,6 +276,13 @@ int fk_batch_set_tile_rows(fk_batch *plan, int rows);
  * (default 0: scalar).  Same bits either way; tuning knobs.  No counterpart in the reference. */
 int fk_batch_set_options(fk_batch *plan, int interleave, int packed);
 
+/* Euler steps per launch of the batched path: 1 (the default), or 2 -- the temporally blocked
+ * kernel on the 32 x 64 work items, each tile advanced two steps between one load and one store
+ * (an odd last step runs alone).  Depth 2 needs every tissue's last tile row and column to hold
+ * more than one cell (H % 32 != 1, W % 64 != 1) and no activation tracking; FK_ERR_ARGUMENT
+ * otherwise.  Same bits either way.  No counterpart in the reference. */
+int fk_batch_set_depth(fk_batch *plan, int depth);
+
 int fk_batch_destroy(fk_batch *plan);
 
 /* ---- reverse mode ---------------------------------------------------------------------------

@@ -92,6 +92,8 @@ def test_autotuner_restores_state_and_picks_a_candidate():
     batch = TissueBatch(b)
     res = tune_batch(batch, trial_steps=32, candidates=(0, 16))
     assert res["graph_steps"] in (0, 16) and res["tile_rows"] in (32, 16)
+    # one tissue (96 x 257) cannot be blocked: depth 1 only
+    assert not batch.can_block() and res["depth"] == 1
     assert len(res["ms_per_step"]) == 16 and batch.tile_rows == res["tile_rows"]
     assert (batch.interleave, batch.packed) == (res["interleave"], res["packed"])
     for t, s in zip(b, before):
@@ -115,3 +117,63 @@ def test_tile_geometry_switches_mid_run_and_ctas_change():
         for p, q in zip(x.view(), y.view()):
             _same(p, q)
     batch.close()
+
+
+def _blockable_tissues(rng):
+    """Mixed shapes, sets and stimuli whose last tile rows and columns hold more than one cell
+    (H % 32 != 1, W % 64 != 1): tiles on every edge, partial tiles, a 3 x 5 grid."""
+    ts = _mixed_tissues(rng)
+    return [t for t in ts if t.H % 32 != 1 and t.W % 64 != 1]
+
+
+@pytest.mark.parametrize("graph_steps,n_steps", [(0, 37), (0, 64), (16, 101), (64, 64)])
+def test_batch_depth_two_matches_single_tissue_bitwise(graph_steps, n_steps):
+    """Two Euler steps per launch (the blocked kernel over the batch's work items; an odd last
+    step alone; graph replays of a multiple of 4 steps) give every tissue the bits of one step
+    per launch."""
+    _gpu()
+    from cardiax_gb300.batch import TissueBatch
+    a = _blockable_tissues(np.random.default_rng(5))
+    b = _blockable_tissues(np.random.default_rng(5))
+    assert len(b) >= 5
+    for t in a:
+        t.advance(0, n_steps)
+    batch = TissueBatch(b, graph_steps=graph_steps)
+    assert batch.can_block()
+    batch.set_depth(2).advance(0, n_steps)
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        for p, q in zip(x.view(), y.view()):
+            _same(p, q)
+    batch.close()
+
+
+def test_batch_depth_two_continues_and_autotunes():
+    """Calls that alternate depth 1 and 2 and odd step counts, then the autotuner over both
+    depths (the state restored)."""
+    _gpu()
+    from cardiax_gb300 import _native as N
+    from cardiax_gb300.autotune import tune_batch
+    from cardiax_gb300.batch import TissueBatch
+    a = _blockable_tissues(np.random.default_rng(6))
+    b = _blockable_tissues(np.random.default_rng(6))
+    for t in a:
+        t.advance(0, 99)
+    batch = TissueBatch(b, graph_steps=8)
+    batch.set_depth(2).advance(0, 13).set_depth(1).advance(13, 40).set_depth(2).advance(40, 99)
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        for p, q in zip(x.view(), y.view()):
+            _same(p, q)
+    before = [t.state.clone() for t in b]
+    res = tune_batch(batch, trial_steps=16, candidates=(0, 8), tile_rows=(32,),
+                     options=((True, False),))
+    assert res["depth"] in (1, 2) and len(res["ms_per_step"]) == 4
+    for t, s in zip(b, before):
+        assert torch.equal(t.state, s)
+    # a batch with a tissue that cannot be blocked refuses depth 2
+    c = TissueBatch(_mixed_tissues(np.random.default_rng(7)))
+    with pytest.raises(N.FkError):
+        c.set_depth(2)
+    batch.close()
+    c.close()
