@@ -30,7 +30,6 @@ namespace fk {
 namespace {
 
 __device__ __forceinline__ int clampi(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
-__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
 // Coefficient of P[m] in row k of G on a padded line of length L (cardiax/solve.py:225-254).
 __device__ __forceinline__ float gcoef(int k, int m, int L) {
@@ -140,32 +139,25 @@ __device__ __forceinline__ float fwd_d2(F at, int i, int N, float rdx) {
     return s * rdx;
 }
 
-// Whether a stimulus replaces the ionic current of cell (i, j) at this step (the replaced J does
-// not depend on the state or theta).  `active`: the stimuli whose protocol is on.
-__device__ __forceinline__ bool stimulated(const AdjointArgs &a, unsigned active, int i, int j,
-                                          int64_t off) {
+// Pointwise part of the adjoint of one cell: cotangents through the gates and currents, and the
+// cell's contribution to dL/dtheta (added into gth).  Returns mu = dt lam'_u.
+__device__ __forceinline__ float adjoint_pointwise(const AdjointArgs &a, int i, int j, int64_t off,
+                                                  float &olv, float &olw, float &olu,
+                                                  float *gth) {
+    const Model &m = a.m;
+    const float dt = a.dt;
+    const float u = __ldg(a.u + off), v = __ldg(a.v + off), w = __ldg(a.w + off);
+    const float lu = __ldg(a.lu + off), lv = __ldg(a.lv + off), lw = __ldg(a.lw + off);
+    const float mu = dt * lu;
     bool stim = false;
     for (int s = 0; s < a.n_stim; ++s) {
-        if (!((active >> s) & 1u)) continue;
+        if (!stim_active(a.stim[s], a.t)) continue;
         const Stim &st = a.stim[s];
         const float fv = st.field ? __ldg(st.field + off)
                                   : ((i >= st.r0 && i < st.r1 && j >= st.c0 && j < st.c1)
                                          ? st.amplitude : 0.0f);
         if (fv != 0.0f) stim = true;
     }
-    return stim;
-}
-
-// Pointwise part of the adjoint of one cell with state (u, v, w) and cotangent (lu, lv, lw) of
-// x_{t+1}: cotangents through the gates and currents, and the cell's contribution to dL/dtheta
-// (added into gth).  Returns mu = dt lam'_u.
-__device__ __forceinline__ float adjoint_pointwise(const AdjointArgs &a, bool stim, float u,
-                                                  float v, float w, float lu, float lv, float lw,
-                                                  float &olv, float &olw, float &olu,
-                                                  float *gth) {
-    const Model &m = a.m;
-    const float dt = a.dt;
-    const float mu = dt * lu;
     const bool p = u >= m.V_c, q = u >= m.V_v;
     const float S = one_plus_tanh(m.k * (u - m.V_csi));  // 1 + tanh
     const float sech2 = S * (2.0f - S);                  // 1 - tanh^2
@@ -184,7 +176,6 @@ __device__ __forceinline__ float adjoint_pointwise(const AdjointArgs &a, bool st
     olv = lv * dvdv + mu * dJdv;
     olw = lw * dwdw + mu * dJdw;
     olu = lu * (1.0f + dt * dJdu);
-    if (!gth) return mu;  // a padding lane of a partial quad
 
     // parameter gradients (cardiax/params.py fields 0..12)
     const float pv = p ? 1.0f : 0.0f, qv = q ? 1.0f : 0.0f;
@@ -350,8 +341,7 @@ __device__ __forceinline__ AxisTerms axis_edge_tab(const float4 *L, const float 
 // Tile geometry: ATY x ATX cells per block, a 4-cell halo of u, D and mu in shared memory.
 constexpr int ATX = 32, ATY = 16, AHALO = 4;
 constexpr int ASW = ATX + 2 * AHALO, ASH = ATY + 2 * AHALO;
-constexpr int ANT = 128;       // one quad (4 adjacent cells of a row) per thread
-constexpr int AQR = ATX / 4;   // quads per tile row
+constexpr int ANT = 256;
 constexpr int AXW = ATX;      // row width of the x-derivative planes (tile rows -2 .. ATY+1)
 constexpr int AYW = ATX + 4;  // row width of the y-derivative planes (tile columns -2 .. ATX+1)
 
@@ -365,8 +355,8 @@ __device__ __forceinline__ void adjoint_tile(const AdjointArgs &a, int bx, int b
     __shared__ __align__(16) float su[ASH * ASW];
     __shared__ __align__(16) float sd[ASH * ASW];
     __shared__ __align__(16) float sm[ASH * ASW];
-    __shared__ __align__(16) float sux[(ATY + 4) * AXW], sqx[(ATY + 4) * AXW], sbx[(ATY + 4) * AXW];
-    __shared__ __align__(16) float suy[ATY * AYW], sqy[ATY * AYW], sby[ATY * AYW];
+    __shared__ float sux[(ATY + 4) * AXW], sqx[(ATY + 4) * AXW], sbx[(ATY + 4) * AXW];
+    __shared__ float suy[ATY * AYW], sqy[ATY * AYW], sby[ATY * AYW];
     __shared__ float red[kAdjParams][ANT / 32];
     // edge band: per line and end, the 10 products each band cell of that line needs (ex: the
     // x-direction lines of the tile's columns, ey: the y-direction lines of its rows), and the
@@ -471,143 +461,50 @@ __device__ __forceinline__ void adjoint_tile(const AdjointArgs &a, int bx, int b
     float gth[kAdjParams];
 #pragma unroll
     for (int k = 0; k < kAdjParams; ++k) gth[k] = 0.0f;
-    unsigned active = 0;
-    for (int q = 0; q < a.n_stim; ++q)
-        if (stim_active(a.stim[q], a.t)) active |= 1u << q;
-    // one quad of 4 adjacent cells of a row per thread: 16-byte loads and stores of the state,
-    // cotangent and dL/dD planes (rows are 16-byte aligned, j is a multiple of 4) and of the
-    // shared derivative planes; per-cell arithmetic as before
-    for (int k = tid; k < ATY * AQR; k += ANT) {
-        const int r = k / AQR, c = 4 * (k % AQR);
+    for (int k = tid; k < ATY * ATX; k += ANT) {
+        const int r = k / ATX, c = k % ATX;
         const int i = i0 + r, j = j0 + c;
         if (i >= H || j >= W) continue;
         const int64_t off = (int64_t)i * pitch + j;
-        const int nv = min(4, W - j);  // cells of the quad inside the grid
-        auto ld = [&](const float *p, float *o) {
-            if (nv == 4) {
-                const float4 x = __ldg(reinterpret_cast<const float4 *>(p + off));
-                o[0] = x.x; o[1] = x.y; o[2] = x.z; o[3] = x.w;
-            } else {
-#pragma unroll
-                for (int m = 0; m < 4; ++m) o[m] = m < nv ? __ldg(p + off + m) : 0.0f;
-            }
-        };
-        float uq[4], vq[4], wq[4], luq[4], lvq[4], lwq[4];
-        {
-            const float4 x = ld4(su + (r + AHALO) * ASW + c + AHALO);  // u = the halo's centre
-            uq[0] = x.x; uq[1] = x.y; uq[2] = x.z; uq[3] = x.w;
-        }
-        ld(a.v, vq);
-        ld(a.w, wq);
-        ld(a.lu, luq);
-        ld(a.lv, lvq);
-        ld(a.lw, lwq);
-        float olv[4], olw[4], olu[4], muq[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            const bool st = active && m < nv && stimulated(a, active, i, j + m, off + m);
-            muq[m] = adjoint_pointwise(a, st, uq[m], vq[m], wq[m], luq[m], lvq[m], lwq[m], olv[m],
-                                       olw[m], olu[m], m < nv ? gth : nullptr);
-        }
-        // x direction (uniform over the quad: one row)
-        AxisTerms xt[4] = {};
+        float olv, olw, olu;
+        const float mu = adjoint_pointwise(a, i, j, off, olv, olw, olu, gth);
+        AxisTerms x, y;
         if (i >= ADJ_BAND && i < H - ADJ_BAND) {
-            auto X = [&](const float *f, int d) { return ld4(f + (r + 2 + d) * AXW + c); };
-            auto M = [&](int d) { return ld4(sm + (r + AHALO + d) * ASW + c + AHALO); };
-            const float4 q0 = X(sqx, -2), q1 = X(sqx, -1), q3 = X(sqx, 1), q4 = X(sqx, 2);
-            const float4 b0 = X(sbx, -2), b1 = X(sbx, -1), b3 = X(sbx, 1), b4 = X(sbx, 2);
-            const float4 u0 = X(sux, -2), u1 = X(sux, -1), u3 = X(sux, 1), u4 = X(sux, 2);
-            const float4 m0 = M(-2), m1 = M(-1), m3 = M(1), m4 = M(2);
-            auto e = [](const float4 &x, int m) { return m == 0 ? x.x : m == 1 ? x.y : m == 2 ? x.z : x.w; };
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                xt[m].AT = g_central(e(q0, m), e(q1, m), e(q3, m), e(q4, m)) * rdx;
-                xt[m].BT = -g_central(e(b0, m), e(b1, m), e(b3, m), e(b4, m)) * rdx;
-                xt[m].d2 = g_central(e(u0, m), e(u1, m), e(u3, m), e(u4, m)) * rdx;
-                xt[m].g = -g_central(e(m0, m) * e(u0, m), e(m1, m) * e(u1, m), e(m3, m) * e(u3, m),
-                                     e(m4, m) * e(u4, m)) * rdx;
-            }
+            auto X = [&](const float *f, int d) { return f[(r + 2 + d) * AXW + c]; };
+            auto M = [&](int d) { return sm[(r + AHALO + d) * ASW + c + AHALO]; };
+            x.AT = g_central(X(sqx, -2), X(sqx, -1), X(sqx, 1), X(sqx, 2)) * rdx;
+            x.BT = -g_central(X(sbx, -2), X(sbx, -1), X(sbx, 1), X(sbx, 2)) * rdx;
+            x.d2 = g_central(X(sux, -2), X(sux, -1), X(sux, 1), X(sux, 2)) * rdx;
+            x.g = -g_central(M(-2) * X(sux, -2), M(-1) * X(sux, -1), M(1) * X(sux, 1),
+                             M(2) * X(sux, 2)) * rdx;
         } else {
             const bool near0 = i < ADJ_BAND;
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                if (m >= nv) continue;
-                if (near0 ? tx0 : tx1)
-                    xt[m] = axis_edge_tab(ex[near0 ? 0 : 1][c + m], tA, tB, near0 ? i : H - 1 - i,
-                                          near0, rdx);
-                else
-                    xt[m] = axis_edge<0>(a, i, j + m);
-            }
+            if (near0 ? tx0 : tx1)
+                x = axis_edge_tab(ex[near0 ? 0 : 1][c], tA, tB, near0 ? i : H - 1 - i, near0, rdx);
+            else
+                x = axis_edge<0>(a, i, j);
         }
-        // y direction: the row's planes at tile columns c-2 .. c+5 (two 16-byte loads each)
-        AxisTerms yt[4] = {};
-        {
-            float fq[8], fb[8], fu[8], fm[12];
-            auto row8 = [&](const float *f, float *o) {
-                const float4 lo = ld4(f + r * AYW + c), hi = ld4(f + r * AYW + c + 4);
-                o[0] = lo.x; o[1] = lo.y; o[2] = lo.z; o[3] = lo.w;
-                o[4] = hi.x; o[5] = hi.y; o[6] = hi.z; o[7] = hi.w;
-            };
-            row8(sqy, fq);
-            row8(sby, fb);
-            row8(suy, fu);
-            {
-                const float *mb = sm + (r + AHALO) * ASW + c + AHALO - 4;  // columns c-4 .. c+7
-                const float4 a0 = ld4(mb), a1 = ld4(mb + 4), a2 = ld4(mb + 8);
-                fm[0] = a0.x; fm[1] = a0.y; fm[2] = a0.z; fm[3] = a0.w;
-                fm[4] = a1.x; fm[5] = a1.y; fm[6] = a1.z; fm[7] = a1.w;
-                fm[8] = a2.x; fm[9] = a2.y; fm[10] = a2.z; fm[11] = a2.w;
-            }
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                if (m >= nv) continue;
-                const int jj = j + m;
-                if (jj >= ADJ_BAND && jj < W - ADJ_BAND) {
-                    // plane column c + m + 2 + d -> fq index m + 2 + d; sm column c + m + d -> fm
-                    // index m + d + 4
-                    yt[m].AT = g_central(fq[m], fq[m + 1], fq[m + 3], fq[m + 4]) * rdx;
-                    yt[m].BT = -g_central(fb[m], fb[m + 1], fb[m + 3], fb[m + 4]) * rdx;
-                    yt[m].d2 = g_central(fu[m], fu[m + 1], fu[m + 3], fu[m + 4]) * rdx;
-                    yt[m].g = -g_central(fm[m + 2] * fu[m], fm[m + 3] * fu[m + 1],
-                                         fm[m + 5] * fu[m + 3], fm[m + 6] * fu[m + 4]) * rdx;
-                } else {
-                    const bool near0 = jj < ADJ_BAND;
-                    if (near0 ? ty0 : ty1)
-                        yt[m] = axis_edge_tab(ey[near0 ? 0 : 1][r], tA, tB,
-                                              near0 ? jj : W - 1 - jj, near0, rdx);
-                    else
-                        yt[m] = axis_edge<1>(a, i, jj);
-                }
-            }
-        }
-        float gDq[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            const float diff_u = (xt[m].AT + yt[m].AT) + (xt[m].BT + yt[m].BT);
-            olu[m] += diff_u;
-            gDq[m] = muq[m] * (xt[m].d2 + yt[m].d2) + (xt[m].g + yt[m].g);
-        }
-        if (nv == 4) {
-            *reinterpret_cast<float4 *>(a.olv + off) = make_float4(olv[0], olv[1], olv[2], olv[3]);
-            *reinterpret_cast<float4 *>(a.olw + off) = make_float4(olw[0], olw[1], olw[2], olw[3]);
-            *reinterpret_cast<float4 *>(a.olu + off) = make_float4(olu[0], olu[1], olu[2], olu[3]);
-            if (a.gD) {
-                float4 *g = reinterpret_cast<float4 *>(a.gD + off);
-                float4 x = *g;
-                x.x += gDq[0];
-                x.y += gDq[1];
-                x.z += gDq[2];
-                x.w += gDq[3];
-                *g = x;
-            }
+        if (j >= ADJ_BAND && j < W - ADJ_BAND) {
+            auto Y = [&](const float *f, int d) { return f[r * AYW + c + 2 + d]; };
+            auto M = [&](int d) { return sm[(r + AHALO) * ASW + c + AHALO + d]; };
+            y.AT = g_central(Y(sqy, -2), Y(sqy, -1), Y(sqy, 1), Y(sqy, 2)) * rdx;
+            y.BT = -g_central(Y(sby, -2), Y(sby, -1), Y(sby, 1), Y(sby, 2)) * rdx;
+            y.d2 = g_central(Y(suy, -2), Y(suy, -1), Y(suy, 1), Y(suy, 2)) * rdx;
+            y.g = -g_central(M(-2) * Y(suy, -2), M(-1) * Y(suy, -1), M(1) * Y(suy, 1),
+                             M(2) * Y(suy, 2)) * rdx;
         } else {
-            for (int m = 0; m < nv; ++m) {
-                a.olv[off + m] = olv[m];
-                a.olw[off + m] = olw[m];
-                a.olu[off + m] = olu[m];
-                if (a.gD) a.gD[off + m] += gDq[m];
-            }
+            const bool near0 = j < ADJ_BAND;
+            if (near0 ? ty0 : ty1)
+                y = axis_edge_tab(ey[near0 ? 0 : 1][r], tA, tB, near0 ? j : W - 1 - j, near0, rdx);
+            else
+                y = axis_edge<1>(a, i, j);
         }
+        const float diff_u = (x.AT + y.AT) + (x.BT + y.BT);
+        const float gD = mu * (x.d2 + y.d2) + (x.g + y.g);
+        a.olv[off] = olv;
+        a.olw[off] = olw;
+        a.olu[off] = olu + diff_u;
+        if (a.gD) a.gD[off] += gD;
     }
 
     // ---- deterministic block reduction of the parameter gradients into this block's slot ----

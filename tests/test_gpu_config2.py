@@ -80,10 +80,12 @@ def test_s1_s2_1e5_steps_512():
     tis = Tissue((H, W), P3, D, gstims)
     tis.track_activation(0.5)
     ck = list(range(0, T + 1, EVERY))
+    stops = sorted(set(ck) | set(legs))  # t1 need not be a checkpoint
     tracked, gsnap = [], {}
-    for a, b in zip(ck[:-1], ck[1:]):
+    for a, b in zip(stops[:-1], stops[1:]):
         tis.advance(a, b)
-        tracked.append(tis.state[..., :W].clone())
+        if b % EVERY == 0:
+            tracked.append(tis.state[..., :W].clone())
         if b in legs:
             gsnap[b] = (tis.view()[2].cpu().numpy(),
                         tuple(x.cpu().numpy().copy() for x in tis.activation_maps()))
