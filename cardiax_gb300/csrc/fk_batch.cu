@@ -141,17 +141,21 @@ bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 // The work list of tile geometry `q` for the plan's work order, and the CTAs' runs of it.
 // Interleaved order: every tissue's edge tiles (the costlier clamped-halo path) first, then the
 // interior tiles, each group with the larger tissues first (CTAs take every G-th item).
-// Contiguous runs: tissue by tissue (larger first), each tissue's tiles row by row, so that a
-// CTA's run changes tissue rarely.
+// Contiguous runs: tissue by tissue (larger first), each tissue's tiles column by column, so
+// that a CTA's run changes tissue rarely and its next item is usually the tile below the
+// current one, whose top halo rows it has just loaded (they are still in L2).
 void build_items(fk_batch *b, int q) {
     fk_batch::PerShape &P = b->sp[q];
     const TileShape &ts = kShape[q];
     P.h_items.clear();
     P.h_edge.clear();
-    auto add = [&](int k, int want_edge) {  // want_edge: 1 edge only, 0 interior only, -1 both
+    // want_edge: 1 edge only, 0 interior only, -1 both; by_column: column-major tile order
+    auto add = [&](int k, int want_edge, bool by_column) {
         const fk_grid &g = b->grids[k];
-        for (int64_t i0 = 0; i0 < g.H; i0 += ts.rows)
-            for (int64_t j0 = 0; j0 < g.W; j0 += ts.cols) {
+        const int64_t nr = (g.H + ts.rows - 1) / ts.rows, nc = (g.W + ts.cols - 1) / ts.cols;
+        for (int64_t a = 0; a < (by_column ? nc : nr); ++a)
+            for (int64_t c = 0; c < (by_column ? nr : nc); ++c) {
+                const int64_t i0 = (by_column ? c : a) * ts.rows, j0 = (by_column ? a : c) * ts.cols;
                 const int edge = interior_tile(g, q, i0, j0) ? 0 : 1;
                 if (want_edge >= 0 && edge != want_edge) continue;
                 P.h_items.push_back(BatchItem{k, (int32_t)i0, (int32_t)j0, 0});
@@ -159,10 +163,10 @@ void build_items(fk_batch *b, int q) {
             }
     };
     if (b->interleave) {
-        for (int k : b->order) add(k, 1);
-        for (int k : b->order) add(k, 0);
+        for (int k : b->order) add(k, 1, false);
+        for (int k : b->order) add(k, 0, false);
     } else {
-        for (int k : b->order) add(k, -1);
+        for (int k : b->order) add(k, -1, true);
     }
     make_ranges(P.h_items, P.h_edge, b->grid, P.h_ranges);
 }
