@@ -58,15 +58,28 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
     if (tid == 0)
         for (int q = 0; q < NSTAGE - 1; ++q)
             if (first + q * stride < stop) issue(first + q * stride, q);
+    // A tissue's arguments are one 32-bit word per thread.  The next item's descriptor is loaded
+    // at the start of an item and, when its tissue differs, that tissue's argument word right
+    // after the item's pass barrier: both loads are in flight while the item computes, and a
+    // tissue change costs a shared-memory store and a barrier.
+    constexpr int AW = (int)(sizeof(StepArgs) / 4);
+    static_assert(AW <= NT, "one argument word per thread");
+    auto arg_word = [&](int tissue) -> uint32_t {
+        return tid < AW
+                   ? __ldg(reinterpret_cast<const uint32_t *>(&tissues[tissue].args[parity]) + tid)
+                   : 0u;
+    };
+    BatchItem b = items[first];
+    uint32_t pw = arg_word(b.tissue);
     int cur = -1, slot = 1;
     unsigned active = 0;
     for (int it = first, n = 0; it < stop; it += stride, ++n) {
         const int s = n % NSTAGE;
-        const BatchItem b = items[it];
+        const BatchItem nb = it + stride < stop ? items[it + stride] : b;
         if (b.tissue != cur) {  // uniform: every thread read the same item
             slot ^= 1;
             StepArgs *sa = reinterpret_cast<StepArgs *>(args + slot * SMEM_ARGS_BYTES);
-            stage_args(sa, &tissues[b.tissue].args[parity]);
+            if (tid < AW) reinterpret_cast<uint32_t *>(sa)[tid] = pw;
             __syncthreads();
             cur = b.tissue;
             active = 0;
@@ -79,6 +92,7 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
         const int ahead = it + (NSTAGE - 1) * stride;
         auto refill = [&] {  // after the pass barrier: item n-1 is done, its stage is free
             if (tid == 0 && ahead < stop) issue(ahead, (n + NSTAGE - 1) % NSTAGE);
+            if (nb.tissue != b.tissue) pw = arg_word(nb.tissue);
         };
         float *ux_n = sux + (n & 1) * (TX * SUX_H), *uy_n = suy + (n & 1) * (SW * TY);
         PairScale ps;
@@ -93,6 +107,7 @@ __global__ void __launch_bounds__(NT, CTAS_PER_SM)
             }
             return;
         }
+        b = nb;
     }
 }
 
