@@ -296,32 +296,46 @@ __device__ __forceinline__ void load_vw(const StepArgs &a, int i0, int j0, TileI
 // columns -2 .. H+1 / W+1), and what is computed for out-of-grid cells is never stored.  Every
 // source cell is inside the grid, hence never a target: one pass, no barrier inside.
 // Buffer row b holds grid row i0 - halo_rows + b, buffer column c grid column j0 - HALO_U + c.
+// Work: the band columns of the in-grid rows, one cell per item (4 or 8 items per row, only for
+// the sides the tile touches), and the band rows as 16-byte groups (a group that straddles a
+// column edge is copied cell by cell).
 static __device__ __noinline__ void clamp_halo(float *buf, int rows, int halo_rows, int i0, int j0,
                                                int H, int W) {
     const int base_r = i0 - halo_rows, base_c = j0 - HALO_U;
-    // band rows: grid rows -4 .. -1 and H .. H+3 inside the buffer; then the in-grid rows
+    // band rows: grid rows -4 .. -1 and H .. H+3 inside the buffer; the in-grid rows between
     const int t_lo = max(0, -4 - base_r), t_hi = min(rows, -base_r);
     const int b_lo = max(0, H - base_r), b_hi = min(rows, H + 4 - base_r);
     const int nt = max(0, t_hi - t_lo), nb = max(0, b_hi - b_lo);
     const int g_lo = max(0, -base_r), g_hi = min(rows, H - base_r);
-    // band columns of the in-grid rows: grid columns -4 .. -1 and W .. W+3 (8 candidates per
-    // row, those outside the buffer skipped)
-    const int n_rows = (nt + nb) * SW, n_cols = max(0, g_hi - g_lo) * 8;
-    for (int it = threadIdx.x; it < n_rows + n_cols; it += NT) {
-        int b, c;
-        if (it < n_rows) {  // whole band rows (corners included)
-            const int rr = it / SW;
-            c = it - rr * SW;
-            b = rr < nt ? t_lo + rr : b_lo + (rr - nt);
-        } else {
-            const int k = it - n_rows, kk = k & 7;
-            b = g_lo + (k >> 3);
-            c = (kk < 4 ? kk - 4 : W + (kk - 4)) - base_c;
-            if (c < 0 || c >= SW) continue;
+    // band columns inside the buffer: [lc0, lc1) left of the grid, [rc0, rc1) right of it
+    const int lc0 = max(0, -4 - base_c), lc1 = max(0, min(SW, -base_c));
+    const int rc0 = max(0, W - base_c), rc1 = min(SW, W + 4 - base_c);
+    const int nl = max(0, lc1 - lc0), nr = max(0, rc1 - rc0);
+    const int sh = (nl > 0 && nr > 0) ? 3 : 2;  // items per in-grid row: 8 (both sides) or 4
+    const int n_cols = (nl + nr > 0) ? max(0, g_hi - g_lo) << sh : 0;
+    constexpr int Q = SW / 4;  // 16-byte groups per buffer row
+    const int n_rows = (nt + nb) * Q;
+    for (int it = threadIdx.x; it < n_cols + n_rows; it += NT) {
+        if (it < n_cols) {
+            const int b = g_lo + (it >> sh), m = it & ((1 << sh) - 1);
+            int c;
+            if (sh == 3) c = m < 4 ? (m < nl ? lc0 + m : -1) : (m - 4 < nr ? rc0 + m - 4 : -1);
+            else if (nl > 0) c = m < nl ? lc0 + m : -1;
+            else c = m < nr ? rc0 + m : -1;
+            if (c < 0) continue;
+            buf[b * SW + c] = buf[b * SW + clampi(base_c + c, 0, W - 1) - base_c];
+        } else {  // whole band rows, corners included
+            const int k = it - n_cols, rr = k / Q, c = 4 * (k - rr * Q);
+            const int b = rr < nt ? t_lo + rr : b_lo + (rr - nt);
+            const float *src = buf + (clampi(base_r + b, 0, H - 1) - base_r) * SW;
+            float *dst = buf + b * SW;
+            if (base_c + c >= 0 && base_c + c + 3 <= W - 1) {
+                st4(dst + c, ld4(src + c));
+            } else {
+#pragma unroll
+                for (int m = 0; m < 4; ++m) dst[c + m] = src[clampi(base_c + c + m, 0, W - 1) - base_c];
+            }
         }
-        const int sb = clampi(base_r + b, 0, H - 1) - base_r;
-        const int sc = clampi(base_c + c, 0, W - 1) - base_c;
-        buf[b * SW + c] = buf[sb * SW + sc];
     }
 }
 
@@ -431,7 +445,7 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
 #pragma unroll
             for (int m = 0; m < 4; ++m) o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]) * rdx;
         }
-        if (EDGE) {
+        if (EDGE && (y0 == 0 || (y0 <= W && W - 1 <= y0 + 3))) {  // few quads
             if (y0 == 0) o[0] = g_head(e[4], e[5], e[6], e[7]) * rdx;  // column 0
 #pragma unroll
             for (int m = 0; m < 4; ++m)  // columns W-1 and W
@@ -726,22 +740,30 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
             jion[2] = js.z;
             jion[3] = js.w;
         }
+        float uyy4[4], dyD4[4];
 #pragma unroll
         for (int m = 0; m < 4; ++m) {
-            float uyy = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
-            float dyD = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
-            if (EDGE) {  // the one-sided rows at column 0 (head) and W-1 (tail)
+            uyy4[m] = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
+            dyD4[m] = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
+        }
+        if (EDGE && (j == 0 || (j <= W - 1 && W - 1 <= j + 3))) {
+            // the one-sided rows at column 0 (head) and W-1 (tail): few quads
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
                 const int y = j + m;
                 if (y == 0) {
-                    uyy = g_head(f[m + 4], f[m + 5], f[m + 6], f[m + 7]);
-                    dyD = g_head(g[m + 4], g[m + 5], g[m + 6], g[m + 7]);
+                    uyy4[m] = g_head(f[m + 4], f[m + 5], f[m + 6], f[m + 7]);
+                    dyD4[m] = g_head(g[m + 4], g[m + 5], g[m + 6], g[m + 7]);
                 } else if (y == W - 1) {
-                    uyy = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]);
-                    dyD = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]);
+                    uyy4[m] = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]);
+                    dyD4[m] = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]);
                 }
             }
-            uyy *= rdx;
-            dyD *= rdx;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const float uyy = uyy4[m] * rdx;
+            const float dyD = dyD4[m] * rdx;
             const float du = diffusion(dd[m], dxv[m], dyD, uxv[m], f[m + 4], uxxv[m], uyy) + jion[m];
             if (DERIV) {
                 ov[m] = dv[m];
