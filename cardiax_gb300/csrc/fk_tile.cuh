@@ -445,11 +445,17 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
 #pragma unroll
             for (int m = 0; m < 4; ++m) o[m] = g_central(e[m + 2], e[m + 3], e[m + 5], e[m + 6]) * rdx;
         }
-        if (EDGE && (y0 == 0 || (y0 <= W && W - 1 <= y0 + 3))) {  // few quads
-            if (y0 == 0) o[0] = g_head(e[4], e[5], e[6], e[7]) * rdx;  // column 0
+        // in an edge tile, few quads: column 0 (head row), columns W-1 and W (tail rows)
+        if (EDGE && y0 == 0) o[0] = g_head(e[4], e[5], e[6], e[7]) * rdx;
+        if (EDGE && y0 <= W && W - 1 <= y0 + 3) {
+            if (y0 + 3 == W - 1) {  // the quad ends at column W-1 (W a multiple of 4)
+                o[3] = g_tail(e[4], e[5], e[6], e[7]) * rdx;
+            } else {
 #pragma unroll
-            for (int m = 0; m < 4; ++m)  // columns W-1 and W
-                if (y0 + m == W - 1 || y0 + m == W) o[m] = g_tail(e[m + 1], e[m + 2], e[m + 3], e[m + 4]) * rdx;
+                for (int m = 0; m < 4; ++m)
+                    if (y0 + m == W - 1 || y0 + m == W)
+                        o[m] = g_tail(e[m + 1], e[m + 2], e[m + 3], e[m + 4]) * rdx;
+            }
         }
         st4(suy + r * SW + HALO_U + 4 * q, make_float4(o[0], o[1], o[2], o[3]));
     }
@@ -544,12 +550,17 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
                     uy4[0] = g_head(f[4], f[5], f[6], f[7]) * rdx;
                     dy4[0] = g_head(g[4], g[5], g[6], g[7]) * rdx;
                 }
+                if (j + 3 == W - 1) {  // the quad ends at column W-1 (W a multiple of 4)
+                    uy4[3] = g_tail(f[4], f[5], f[6], f[7]) * rdx;
+                    dy4[3] = g_tail(g[4], g[5], g[6], g[7]) * rdx;
+                } else {
 #pragma unroll
-                for (int m = 0; m < 4; ++m)
-                    if (j + m == W - 1) {
-                        uy4[m] = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]) * rdx;
-                        dy4[m] = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]) * rdx;
-                    }
+                    for (int m = 0; m < 3; ++m)
+                        if (j + m == W - 1) {
+                            uy4[m] = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]) * rdx;
+                            dy4[m] = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]) * rdx;
+                        }
+                }
                 uyy_lo = mk2(uy4[0], uy4[1]);
                 uyy_hi = mk2(uy4[2], uy4[3]);
                 dyD_lo = mk2(dy4[0], dy4[1]);
@@ -746,18 +757,22 @@ __device__ __forceinline__ bool compute_tile(const StepArgs &a, const PackConsts
             uyy4[m] = g_central(f[m + 2], f[m + 3], f[m + 5], f[m + 6]);
             dyD4[m] = g_central(g[m + 2], g[m + 3], g[m + 5], g[m + 6]);
         }
-        if (EDGE && (j == 0 || (j <= W - 1 && W - 1 <= j + 3))) {
-            // the one-sided rows at column 0 (head) and W-1 (tail): few quads
+        // in an edge tile, few quads: the one-sided rows at column 0 (head) and W-1 (tail)
+        if (EDGE && j == 0) {
+            uyy4[0] = g_head(f[4], f[5], f[6], f[7]);
+            dyD4[0] = g_head(g[4], g[5], g[6], g[7]);
+        }
+        if (EDGE && j <= W - 1 && W - 1 <= j + 3) {
+            if (j + 3 == W - 1) {  // the quad ends at column W-1 (W a multiple of 4)
+                uyy4[3] = g_tail(f[4], f[5], f[6], f[7]);
+                dyD4[3] = g_tail(g[4], g[5], g[6], g[7]);
+            } else {
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                const int y = j + m;
-                if (y == 0) {
-                    uyy4[m] = g_head(f[m + 4], f[m + 5], f[m + 6], f[m + 7]);
-                    dyD4[m] = g_head(g[m + 4], g[m + 5], g[m + 6], g[m + 7]);
-                } else if (y == W - 1) {
-                    uyy4[m] = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]);
-                    dyD4[m] = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]);
-                }
+                for (int m = 0; m < 3; ++m)
+                    if (j + m == W - 1) {
+                        uyy4[m] = g_tail(f[m + 1], f[m + 2], f[m + 3], f[m + 4]);
+                        dyD4[m] = g_tail(g[m + 1], g[m + 2], g[m + 3], g[m + 4]);
+                    }
             }
         }
 #pragma unroll
@@ -815,6 +830,11 @@ __device__ __forceinline__ bool is_sliver(int i0, int j0, int H, int W) {
     return H - i0 < 2 || W - j0 < 2;
 }
 
+// A tile within BAND of a grid edge (a clamped edge tile, or a sliver).
+__device__ __forceinline__ bool edge_tile(int i0, int j0, int H, int W) {
+    return !(i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND);
+}
+
 // Interior tiles, clamped edge tiles, or slivers (interior passes + per-cell band).
 // PK: packed arithmetic with the launch's constants *pk (null when !PK).
 // DIRECT: see compute_tile; returns false when the tile was abandoned (a failed TMA wait).
@@ -828,8 +848,7 @@ __device__ __forceinline__ bool process_tile(const StepArgs &a, float t, const S
                                              PairScale ps = PairScale{}, bool ok = true,
                                              P2 &&after_barrier = P2{}) {
     const int H = a.H, W = a.W;
-    const bool interior = i0 >= BAND && i0 + TY <= H - BAND && j0 >= BAND && j0 + TX <= W - BAND;
-    if (interior) {
+    if (!edge_tile(i0, j0, H, W)) {
         return compute_tile<DERIV, ACT, false, PK, DIRECT, HEUN>(a, pk, ps, t, st, sux, suy, io, active,
                                                                  i0, j0, after_pass1, ok,
                                                                  after_barrier);
