@@ -640,7 +640,8 @@ def run_schedules(dev, sizes=(256, 512, 1024, 2048), steps: int = 400):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     from cardiax_gb300 import autotune
     modes = {"k1": {}, "k2": {"depth": 2}, "k4": {"depth": 4}, "k8": {"depth": 8},
-             "flow": {"schedule": "flow"}, "auto": {"schedule": "auto"}}
+             "flow": {"schedule": "flow"}, "batch16": {"schedule": "batch", "tile_rows": 16},
+             "auto": {"schedule": "auto"}}
     out = {}
     for size in sizes:
         D, field, proto = workload(size, size)
@@ -665,7 +666,9 @@ def run_schedules(dev, sizes=(256, 512, 1024, 2048), steps: int = 400):
             if name == "auto":
                 sched, depth, kernel = autotune.tune_tissue(tis)["choice"]
                 row[name]["choice"] = {"schedule": sched, "depth": depth,
-                                       "kernel": "strip" if kernel else "tiled"}
+                                       "kernel": (f"batched, {kernel}-row items"
+                                                  if sched == "batch" else
+                                                  "strip" if kernel else "tiled")}
         out[f"{size}x{size}"] = row
     return out
 

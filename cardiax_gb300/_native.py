@@ -11,7 +11,9 @@ import threading
 
 from . import _build
 
-FK_MAX_STIMULI = 8
+# include/cardiax_gb300.h: stimuli per call, and stimuli active at once within one launch
+FK_MAX_STIMULI = 64
+FK_MAX_ACTIVE_STIMULI = 8
 
 
 class FkError(RuntimeError):

@@ -28,8 +28,10 @@ _CACHE: dict = {}
 _TISSUE_CACHE: dict = {}
 
 # (schedule, depth, step kernel) candidates of tune_tissue; step kernel 0 = tiled, 1 = strip
+# (schedule, depth, third): the step kernel (0 tiled, 1 strip) for "step" and "flow", the work
+# item rows for "batch" (the batched kernel on the one tissue)
 TISSUE_CANDIDATES = (("step", 1, 0), ("step", 1, 1), ("step", 2, 0), ("step", 4, 0),
-                     ("step", 8, 0), ("flow", 1, 0))
+                     ("step", 8, 0), ("flow", 1, 0), ("batch", 1, 16), ("batch", 1, 32))
 
 GRAPH_CANDIDATES = (0, 64)
 TILE_ROW_CANDIDATES = (32, 16)
@@ -108,6 +110,9 @@ def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CAND
 
 def _run(tis, t0: int, t1: int, choice) -> None:
     schedule, depth, kernel = choice
+    if schedule == "batch":
+        tis.advance(t0, t1, schedule="batch", tile_rows=kernel)
+        return
     if kernel:
         N.call("fk_select_step_kernel", int(kernel))
     try:
@@ -123,7 +128,8 @@ def _run(tis, t0: int, t1: int, choice) -> None:
 def tune_tissue(tis, trial_steps: int = 64, candidates=TISSUE_CANDIDATES,
                 verbose: bool = False) -> dict:
     """The fastest way to step ``tis`` (a :class:`~cardiax_gb300.tissue.Tissue`): returns
-    ``{"choice": (schedule, depth, step_kernel), "us_per_step": {choice: us}}``; the tissue's
+    ``{"choice": (schedule, depth, step_kernel or tile rows), "us_per_step": {choice: us}}``
+    (candidates: ``TISSUE_CANDIDATES``); the tissue's
     state is restored.  With activation tracking on, only one-step-per-launch candidates
     qualify (temporal blocking does not track activations)."""
     tracking = tis.activation is not None

@@ -154,8 +154,9 @@ Model make_model(const fk_params &p) {
     return m;
 }
 
-int make_stims(const fk_stimulus *s, int n, const fk_grid &g, Stim *out) {
-    if (n < 0 || n > FK_MAX_STIMULI || n > kMaxStim) return FK_ERR_STIMULI;
+static_assert(kMaxStim == FK_MAX_ACTIVE_STIMULI, "kernel stimulus slots");
+
+static int convert_stims(const fk_stimulus *s, int n, const fk_grid &g, Stim *out) {
     if (n > 0 && !s) return FK_ERR_NULL;
     for (int k = 0; k < n; ++k) {
         if (!std::isfinite(s[k].start) || !std::isfinite(s[k].duration) ||
@@ -178,6 +179,44 @@ int make_stims(const fk_stimulus *s, int n, const fk_grid &g, Stim *out) {
             o.c1 = s[k].c1 > g.W ? (int32_t)g.W : s[k].c1;
         }
     }
+    return FK_OK;
+}
+
+int make_stims(const fk_stimulus *s, int n, const fk_grid &g, Stim *out) {
+    if (n < 0 || n > kMaxStim) return FK_ERR_STIMULI;
+    return convert_stims(s, n, g, out);
+}
+
+// The protocol test of the kernels (stim_active in fk_math.cuh), on the host: the same float32
+// operations, so the host and the device agree on every step.
+static bool stim_active_host(const Stim &s, float t) {
+    if (!(t >= s.start)) return false;
+    const float a = (s.start - t) + 1.0f;
+    float m = std::fmod(a, s.period);
+    if (m != 0.0f && ((s.period < 0.0f) != (m < 0.0f))) m += s.period;
+    return m < s.duration;
+}
+
+int StimList::make(const fk_stimulus *s, int count, const fk_grid &g) {
+    if (count < 0 || count > FK_MAX_STIMULI) return FK_ERR_STIMULI;
+    n = count;
+    return convert_stims(s, count, g, all);
+}
+
+int StimList::window(int64_t t0, int64_t t1, Stim *out, int *ns) const {
+    int k = 0;
+    for (int i = 0; i < n; ++i) {
+        bool can = fixed();
+        if (!can && t1 - t0 <= 64) {  // short windows: step by step
+            for (int64_t t = t0; t < t1 && !can; ++t) can = stim_active_host(all[i], (float)t);
+        } else if (!can) {  // long windows: any stimulus that has started by the last step
+            can = (float)(t1 - 1) >= all[i].start;
+        }
+        if (!can) continue;
+        if (k == kMaxStim) return FK_ERR_STIMULI;
+        out[k++] = all[i];
+    }
+    *ns = k;
     return FK_OK;
 }
 
@@ -483,14 +522,16 @@ int fk_step(fk_grid g, const float *state, const float *D, const fk_params *p,
             void *stream) {
     int rc = common_checks(g, state, dstate, D, p, dx);
     if (rc) return rc;
+    StimList L;
     Stim st[kMaxStim];
-    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    int ns = 0;
+    if ((rc = L.make(stimuli, n_stimuli, g)) || (rc = L.window(t, t + 1, st, &ns))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
     if (!status) return FK_ERR_CUDA;
     MapCache maps;
-    return step_once(g, state, dstate, D, make_model(*p), st, n_stimuli, t, 0.0f,
+    return step_once(g, state, dstate, D, make_model(*p), st, ns, t, 0.0f,
                      1.0f / (float)dx, true, tm_d, maps, status, (cudaStream_t)stream);
 }
 
@@ -500,14 +541,16 @@ int fk_euler_step(fk_grid g, const float *state, const float *D, const fk_params
     int rc = common_checks(g, state, state_out, D, p, dx);
     if (rc) return rc;
     if (!std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    StimList L;
     Stim st[kMaxStim];
-    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    int ns = 0;
+    if ((rc = L.make(stimuli, n_stimuli, g)) || (rc = L.window(t, t + 1, st, &ns))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
     if (!status) return FK_ERR_CUDA;
     MapCache maps;
-    return step_once(g, state, state_out, D, make_model(*p), st, n_stimuli, t, (float)dt,
+    return step_once(g, state, state_out, D, make_model(*p), st, ns, t, (float)dt,
                      1.0f / (float)dx, false, tm_d, maps, status, (cudaStream_t)stream);
 }
 
@@ -522,8 +565,10 @@ int fk_forward_euler_tracked(fk_grid g, float *state, float *scratch, const floa
         if (!act->first || !act->last || !act->count) return FK_ERR_NULL;
         if (!std::isfinite(act->threshold)) return FK_ERR_ARGUMENT;
     }
+    StimList L;
     Stim st[kMaxStim];
-    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    int ns = 0;
+    if ((rc = L.make(stimuli, n_stimuli, g)) || (rc = L.window(t0, t0 + 1, st, &ns))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
@@ -535,7 +580,8 @@ int fk_forward_euler_tracked(fk_grid g, float *state, float *scratch, const floa
     MapCache maps;
     for (int64_t t = t0; t < t1; ++t) {
         const int k = (int)((t - t0) & 1);
-        rc = step_once(g, bufs[k], bufs[k ^ 1], D, m, st, n_stimuli, t, (float)dt, rdx, false,
+        if (!L.fixed() && (rc = L.window(t, t + 1, st, &ns))) return rc;
+        rc = step_once(g, bufs[k], bufs[k ^ 1], D, m, st, ns, t, (float)dt, rdx, false,
                        tm_d, maps, status, s, act);
         if (rc) return rc;
     }
@@ -569,13 +615,15 @@ int fk_forward_euler_flow(fk_grid g, const float *src, float *dst, float *scratc
         if (!act->first || !act->last || !act->count) return FK_ERR_NULL;
         if (!std::isfinite(act->threshold)) return FK_ERR_ARGUMENT;
     }
+    StimList L;
     Stim st[kMaxStim];
-    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    int ns = 0;
+    if ((rc = L.make(stimuli, n_stimuli, g)) || (rc = L.window(t0, t1, st, &ns))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
     if (!status) return FK_ERR_CUDA;
-    return flow_run(g, src, dst, scratch, D, tm_d, make_model(*p), st, n_stimuli, t0, t1 - t0,
+    return flow_run(g, src, dst, scratch, D, tm_d, make_model(*p), st, ns, t0, t1 - t0,
                     (float)dt, 1.0f / (float)dx, act, flags, status, (cudaStream_t)stream);
 }
 
@@ -591,8 +639,8 @@ int fk_forward_flow(fk_grid g, const float *state0, float *scratch, const float 
     if (n_flags < flow_flag_words(g.H, g.W)) return FK_ERR_ARGUMENT;
     for (int i = 0; i + 1 < n_checkpoints; ++i)
         if (checkpoints[i + 1] < checkpoints[i]) return FK_ERR_ARGUMENT;
-    Stim st[kMaxStim];
-    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    StimList L;
+    if ((rc = L.make(stimuli, n_stimuli, g))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
@@ -603,7 +651,10 @@ int fk_forward_flow(fk_grid g, const float *state0, float *scratch, const float 
     for (int i = 0; i + 1 < n_checkpoints; ++i) {
         float *dst = out + (int64_t)i * n_state;
         if (dst == scratch || cur == scratch) return FK_ERR_ARGUMENT;
-        if ((rc = flow_run(g, cur, dst, scratch, D, tm_d, m, st, n_stimuli, checkpoints[i],
+        Stim st[kMaxStim];
+        int ns = 0;
+        if ((rc = L.window(checkpoints[i], checkpoints[i + 1], st, &ns))) return rc;
+        if ((rc = flow_run(g, cur, dst, scratch, D, tm_d, m, st, ns, checkpoints[i],
                            checkpoints[i + 1] - checkpoints[i], (float)dt, 1.0f / (float)dx,
                            nullptr, flags, status, (cudaStream_t)stream)))
             return rc;
@@ -625,8 +676,10 @@ int fk_forward_euler_tb(fk_grid g, float *state, float *scratch, const float *D,
     if (depth == 1 || g.H % oh == 1 || g.W % ow == 1)
         return fk_forward_euler(g, state, scratch, D, p, stimuli, n_stimuli, t0, t1, dt, dx,
                                 stream);
+    StimList L;
     Stim st[kMaxStim];
-    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    int ns = 0;
+    if ((rc = L.make(stimuli, n_stimuli, g)) || (rc = L.window(t0, t0 + 1, st, &ns))) return rc;
     int *status = status_ptr();
     if (!status) return FK_ERR_CUDA;
     const Model m = make_model(*p);
@@ -656,12 +709,14 @@ int fk_forward_euler_tb(fk_grid g, float *state, float *scratch, const float *D,
     int64_t t = t0;
     for (; t + depth <= t1; t += depth) {
         StepArgs a;
-        fill_args(a, g, bufs[cur], D, m, st, n_stimuli, (float)dt, rdx, status, nullptr);
+        if (!L.fixed() && (rc = L.window(t, t + depth, st, &ns))) return rc;
+        fill_args(a, g, bufs[cur], D, m, st, ns, (float)dt, rdx, status, nullptr);
         if (launch_tb(depth, tm[cur], a, t, s) != cudaSuccess) return FK_ERR_CUDA;
         cur ^= 1;
     }
     for (; t < t1; ++t) {  // the remainder, one step per launch
-        if ((rc = step_once(g, bufs[cur], bufs[cur ^ 1], D, m, st, n_stimuli, t, (float)dt, rdx,
+        if (!L.fixed() && (rc = L.window(t, t + 1, st, &ns))) return rc;
+        if ((rc = step_once(g, bufs[cur], bufs[cur ^ 1], D, m, st, ns, t, (float)dt, rdx,
                             false, tm_d, maps, status, s)))
             return rc;
         cur ^= 1;
@@ -703,14 +758,16 @@ int fk_heun_step(fk_grid g, const float *state, const float *D, const fk_params 
     if (!work) return FK_ERR_NULL;
     if (!aligned16(work)) return FK_ERR_ALIGN;
     if (!std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    StimList L;
     Stim st[kMaxStim];
-    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    int ns = 0;
+    if ((rc = L.make(stimuli, n_stimuli, g)) || (rc = L.window(t, t + 1, st, &ns))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
     if (!status) return FK_ERR_CUDA;
     MapCache maps;
-    return heun_once(g, state, state_out, work, D, make_model(*p), st, n_stimuli, t, (float)dt,
+    return heun_once(g, state, state_out, work, D, make_model(*p), st, ns, t, (float)dt,
                      1.0f / (float)dx, tm_d, maps, status, (cudaStream_t)stream);
 }
 
@@ -720,8 +777,10 @@ int fk_forward_heun(fk_grid g, float *state, float *work, const float *D, const 
     int rc = common_checks(g, state, work, D, p, dx);
     if (rc) return rc;
     if (t1 < t0 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
+    StimList L;
     Stim st[kMaxStim];
-    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    int ns = 0;
+    if ((rc = L.make(stimuli, n_stimuli, g)) || (rc = L.window(t0, t0 + 1, st, &ns))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
@@ -735,7 +794,8 @@ int fk_forward_heun(fk_grid g, float *state, float *work, const float *D, const 
     MapCache maps;
     for (int64_t t = t0; t < t1; ++t) {
         const int k = (int)((t - t0) & 1);
-        if ((rc = heun_once(g, bufs[k], bufs[k ^ 1], work, D, m, st, n_stimuli, t, (float)dt, rdx,
+        if (!L.fixed() && (rc = L.window(t, t + 1, st, &ns))) return rc;
+        if ((rc = heun_once(g, bufs[k], bufs[k ^ 1], work, D, m, st, ns, t, (float)dt, rdx,
                             tm_d, maps, status, s)))
             return rc;
     }
@@ -756,8 +816,10 @@ int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
     if (n_checkpoints < 1 || !std::isfinite(dt)) return FK_ERR_ARGUMENT;
     for (int i = 0; i + 1 < n_checkpoints; ++i)
         if (checkpoints[i + 1] < checkpoints[i]) return FK_ERR_ARGUMENT;
+    StimList L;
     Stim st[kMaxStim];
-    if ((rc = make_stims(stimuli, n_stimuli, g, st))) return rc;
+    int ns = 0;
+    if ((rc = L.make(stimuli, n_stimuli, g)) || (rc = L.window(0, 1, st, &ns))) return rc;
     CUtensorMap tm_d;
     if ((rc = make_plane_map(&tm_d, D, g.H, g.W, g.pitch, SW, SD_H))) return rc;
     int *status = status_ptr();
@@ -779,7 +841,8 @@ int fk_forward(fk_grid g, const float *state0, float *scratch, const float *D,
         // ping-pong so that the interval's last step lands in dst
         for (int64_t k = 0; k < n; ++k) {
             float *o = ((n - 1 - k) & 1) ? scratch : dst;
-            rc = step_once(g, cur, o, D, m, st, n_stimuli, a + k, (float)dt, rdx, false, tm_d,
+            if (!L.fixed() && (rc = L.window(a + k, a + k + 1, st, &ns))) return rc;
+            rc = step_once(g, cur, o, D, m, st, ns, a + k, (float)dt, rdx, false, tm_d,
                            maps, status, s);
             if (rc) return rc;
             cur = o;

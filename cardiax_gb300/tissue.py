@@ -106,7 +106,8 @@ def stimulus_table(stimuli: Sequence, H: int, W: int, pitch: int, device):
             keep.append(p)
             entries.append(N.Stimulus(start, duration, period, p.data_ptr(), 0, 0, 0, 0, 0.0))
     if len(entries) > N.FK_MAX_STIMULI:
-        raise ValueError(f"at most {N.FK_MAX_STIMULI} non-zero stimuli are supported per tissue")
+        raise ValueError(f"at most {N.FK_MAX_STIMULI} non-zero stimuli are supported per tissue "
+                         f"(of which at most {N.FK_MAX_ACTIVE_STIMULI} active at one step)")
     arr = (N.Stimulus * max(1, len(entries)))(*entries)
     return arr, len(entries), keep
 
@@ -135,6 +136,7 @@ class Tissue:
             self.state = torch.empty((3, H, self.pitch), dtype=torch.float32, device=self.device)
             self.scratch = torch.empty_like(self.state)
         self.activation = None
+        self._batches = {}  # one-tissue batch plans by tile rows (schedule="batch")
         self.init()
 
     # -- state ----------------------------------------------------------------------------
@@ -164,7 +166,13 @@ class Tissue:
         self.act_count = torch.zeros((self.H, self.pitch), **kw)
         self.activation = N.Activation(self.act_first.data_ptr(), self.act_last.data_ptr(),
                                        self.act_count.data_ptr(), float(threshold))
+        self._drop_batches()  # their plans were built without tracking
         return self
+
+    def _drop_batches(self):
+        for b in self._batches.values():
+            b.close()
+        self._batches = {}
 
     def activation_maps(self):
         """(first, last, count) activation maps without the padding columns."""
@@ -180,13 +188,33 @@ class Tissue:
             self._flags = torch.zeros(n, dtype=torch.int32, device=self.device)
         return self._flags
 
-    def advance(self, t0: int, t1: int, schedule: str = "step", depth: int = 1) -> "Tissue":
+    def _one_batch(self, tile_rows: int):
+        """A batch plan holding this tissue alone, with ``tile_rows`` x 64 work items (kept
+        until activation tracking changes)."""
+        from .batch import TissueBatch
+        b = self._batches.get(tile_rows)
+        if b is None:
+            b = TissueBatch([self], tile_rows=tile_rows)
+            self._batches[tile_rows] = b
+        return b
+
+    def advance(self, t0: int, t1: int, schedule: str = "step", depth: int = 1,
+                tile_rows: int = 16) -> "Tissue":
         """Steps t0 .. t1-1 in place (cardiax/solve.py:92-100).  ``schedule="step"``: one launch
         per step (chained with programmatic dependent launch), or with ``depth`` 2, 4 or 8 that
         many steps per launch (temporal blocking); ``"flow"``: one cooperative dataflow launch
-        for the whole range; ``"auto"``: whichever of these (and of the tiled and strip step
-        kernels) ``autotune.tune_tissue`` measured fastest on this grid.  All give identical
-        results."""
+        for the whole range; ``"batch"``: the batched kernel on this tissue alone, with
+        ``tile_rows`` x 64 work items (16-row items put twice the CTAs on a small grid and
+        shorten each step's critical path) and CUDA-graph replay; ``"auto"``: whichever of these
+        (and of the tiled and strip step kernels) ``autotune.tune_tissue`` measured fastest on
+        this grid.  All give identical results.  With more stimuli than one launch holds
+        (``FK_MAX_ACTIVE_STIMULI``) each launch takes the stimuli that can be active during its
+        steps, so ``"flow"``, ``"batch"`` and ``"auto"`` step one launch per step instead."""
+        if self.n_stim > N.FK_MAX_ACTIVE_STIMULI and schedule in ("flow", "batch", "auto"):
+            schedule, depth = "step", 1
+        if schedule == "batch":
+            self._one_batch(int(tile_rows)).advance(t0, t1)
+            return self
         if schedule == "auto":
             from . import autotune
             autotune._run(self, t0, t1, autotune.tune_tissue(self)["choice"])
@@ -238,7 +266,7 @@ class Tissue:
         if n == 0:
             return out
         arr = (ctypes.c_int64 * len(ck))(*ck)
-        if schedule == "step":
+        if schedule == "step" or self.n_stim > N.FK_MAX_ACTIVE_STIMULI:
             N.call("fk_forward", self.grid, self.state.data_ptr(), self.scratch.data_ptr(),
                    self.D.data_ptr(), ctypes.byref(self.params), self.stim, self.n_stim, arr,
                    len(ck), self.dt, self.dx, out.data_ptr(), stream_handle())

@@ -63,7 +63,16 @@ typedef struct {
     float amplitude;
 } fk_stimulus;
 
-#define FK_MAX_STIMULI 8
+/* A call takes up to FK_MAX_STIMULI stimuli.  At most FK_MAX_ACTIVE_STIMULI of them may be
+ * active at any one step of a call that launches one kernel per step (fk_step, fk_euler_step,
+ * fk_forward_euler[_tracked], fk_forward, fk_heun_step, fk_forward_heun, and the one-step
+ * remainder of fk_forward_euler_tb): the library passes each launch the stimuli active at its
+ * step, in list order.  Calls that advance several steps per launch (fk_forward_euler_tb,
+ * fk_forward_euler_flow, fk_forward_flow, the batch and the adjoint) need the stimuli that can
+ * be active anywhere in a launch's steps to number at most FK_MAX_ACTIVE_STIMULI (for the batch
+ * and the adjoint: a tissue's whole list).  More: FK_ERR_STIMULI. */
+#define FK_MAX_STIMULI 64
+#define FK_MAX_ACTIVE_STIMULI 8
 
 typedef struct {
     int64_t H, W, pitch;

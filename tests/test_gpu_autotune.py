@@ -10,13 +10,13 @@ pytestmark = pytest.mark.gpu
 P3 = (3.33, 19.6, 1250, 870, 41, 0.25, 12.5, 33.33, 29, 10, 0.85, 0.13, 0.04, 1)
 
 
-def _tissue(H, W, seed):
+def _tissue(H, W, seed, cols=4, amplitude=20.0):
     from cardiax_gb300.stimulus import Protocol, Stimulus
     from cardiax_gb300.tissue import Tissue
     rng = np.random.default_rng(seed)
     D = (1e-3 * (1 + 0.05 * rng.standard_normal((H, W)))).astype(np.float32)
     f = np.zeros((H, W), np.float32)
-    f[:, :4] = 20.0
+    f[:, :cols] = amplitude
     return Tissue((H, W), P3, np.clip(D, 0, None), [Stimulus(Protocol(0, 2, 1e9), f)])
 
 
@@ -47,3 +47,30 @@ def test_tracking_restricts_the_candidates():
     t.advance(0, 50, schedule="auto")
     torch.cuda.synchronize()
     assert int((t.act_first[:, :64] >= 0).sum()) > 0
+
+
+@pytest.mark.parametrize("H,W", [(37, 90), (128, 128), (200, 64)])
+def test_one_tissue_batch_schedule_is_bit_identical(H, W):
+    """schedule="batch" (the batched kernel on the one tissue, 16- or 32-row items, graph
+    replay plus a remainder) steps exactly as the default, activation maps included."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    a, b = _tissue(H, W, 1), _tissue(H, W, 1)
+    for rows in (16, 32):
+        a.init()
+        b.init()
+        a.advance(0, 77, schedule="batch", tile_rows=rows).advance(77, 150, schedule="batch",
+                                                                    tile_rows=rows)
+        b.advance(0, 150)
+        torch.cuda.synchronize()
+        assert torch.equal(a.state[:, :, :W], b.state[:, :, :W]), rows
+    # a 10-column strip at 50 starts a wave (4 columns at 20 stay below threshold)
+    c = _tissue(H, W, 2, cols=10, amplitude=50.0).track_activation(0.5)
+    d = _tissue(H, W, 2, cols=10, amplitude=50.0).track_activation(0.5)
+    c.advance(0, 150, schedule="batch")
+    d.advance(0, 150)
+    torch.cuda.synchronize()
+    assert torch.equal(c.state[:, :, :W], d.state[:, :, :W])
+    for x, y in zip(c.activation_maps(), d.activation_maps()):
+        assert torch.equal(x, y)
+    assert int((c.act_first[:, :W] >= 0).sum()) > 0

@@ -179,18 +179,83 @@ def test_forward_is_deterministic_and_matches_stepwise():
         assert torch.equal(p, q)
 
 
-def test_too_many_stimuli_rejected():
+def _staggered_stimuli(shp, n, seed):
+    """n stimuli (rectangles and dense fields) whose protocols overlap in time a few at once."""
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    rng = np.random.default_rng(seed)
+    H, W = shp
+    out_g, out_o = [], []
+    for k in range(n):
+        f = np.zeros(shp, np.float32)
+        r, c = int(rng.integers(0, H - 6)), int(rng.integers(0, W - 6))
+        if k % 3 == 2:  # a field with two values: a dense plane
+            f[r:r + 6, c:c + 3] = 6.0 + k
+            f[r:r + 6, c + 3:c + 6] = 2.0
+        else:
+            f[r:r + 6, c:c + 6] = 4.0 + k
+        start, dur, period = 7 * k, 3, 40 + 5 * (k % 4)
+        out_g.append(Stimulus(Protocol(start, dur, period), f))
+        out_o.append(O.OStim(start, dur, period, f))
+    return out_g, out_o
+
+
+def test_more_stimuli_than_a_launch_holds_vs_oracle():
+    """20 stimuli, a few active at any step: each launch takes the ones active at its step (in
+    list order, overlaps included); 300 Euler and 60 Heun steps against the oracle, and every
+    schedule gives the per-step bits."""
     _gpu()
     from cardiax_gb300 import solve
+    from cardiax_gb300.tissue import Tissue
+    shp = (48, 72)
+    rng = np.random.default_rng(5)
+    D = _smooth(rng, shp, 4e-4, 1e-3)
+    stims_g, stims_o = _staggered_stimuli(shp, 20, 3)
+    got = solve._forward_euler(solve.init(shp), 0, 300, P3, D, stims_g, 0.01, 0.01)
+    ref = O.forward_euler(O.init(shp), 0, 300, P3, D, stims_o, 0.01, 0.01)
+    worst = max(float(np.abs(_np(a) - b).max()) for a, b in zip(got, ref))
+    assert worst <= 1e-4, worst
+    assert float(got.u.max()) > 0.5  # the stimuli excited the tissue
+    d = solve.step(solve.init(shp), 21, P3, D, stims_g, 0.01)
+    d_ref = O.derivative(O.init(shp), np.float32(21), P3, D, stims_o, 0.01)
+    assert np.abs(_np(d.u) - d_ref.u).max() <= 1e-4
+    h = solve._forward_heun(solve.init(shp), 0, 60, P3, D, stims_g, 0.01, 0.01)
+    h_ref = O.forward_heun(O.init(shp), 0, 60, P3, D, stims_o, 0.01, 0.01)
+    assert max(float(np.abs(_np(a) - b).max()) for a, b in zip(h, h_ref)) <= 1e-4
+    ck = [0, 50, 120, 300]
+    fw = solve.forward(solve.init(shp), ck, P3, D, stims_g, 0.01, 0.01)
+    for p, q in zip(fw[-1], got):
+        assert torch.equal(p, q)
+    for kw in ({"schedule": "flow"}, {"depth": 2}, {"schedule": "auto"}):
+        t = Tissue(shp, P3, D, stims_g)
+        t.advance(0, 300, **kw)
+        for p, q in zip(t.view(), got):
+            assert torch.equal(p, q), kw
+    print(f"20 stimuli, 300 steps: max|d| vs oracle {worst:.3g}")
+
+
+def test_too_many_stimuli_rejected():
+    """Nine stimuli active at the same step exceed a launch's slots (FkError from the library);
+    more than FK_MAX_STIMULI non-zero stimuli are refused before any launch (ValueError)."""
+    _gpu()
+    from cardiax_gb300 import solve
+    from cardiax_gb300._native import FK_MAX_STIMULI, FkError
     from cardiax_gb300.stimulus import Protocol, Stimulus
     shp = (16, 16)
+    D = np.full(shp, 1e-3, np.float32)
     stims = []
     for k in range(9):
         f = np.zeros(shp, np.float32)
         f[k, :] = 1.0
         stims.append(Stimulus(Protocol(0, 2, 5), f))
+    with pytest.raises(FkError):
+        solve._forward_euler(solve.init(shp), 0, 3, P3, D, stims, 0.01, 0.01)
+    many = []
+    for k in range(FK_MAX_STIMULI + 1):
+        f = np.zeros(shp, np.float32)
+        f[k % 16, k // 16] = 1.0
+        many.append(Stimulus(Protocol(1000 * k, 2, 1e9), f))
     with pytest.raises(ValueError):
-        solve._forward_euler(solve.init(shp), 0, 3, P3, np.full(shp, 1e-3, np.float32), stims, 0.01, 0.01)
+        solve._forward_euler(solve.init(shp), 0, 3, P3, D, many, 0.01, 0.01)
 
 
 def _c_oracle():
