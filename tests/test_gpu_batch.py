@@ -18,6 +18,8 @@ def _same(p, q):
 
 
 def _mixed_tissues(rng, track=False):
+    """Seven tissues of different shapes (3 x 5 .. 256 x 130), parameter sets, D maps,
+    stimuli, time steps and cell sizes."""
     from cardiax_gb300 import params as Pm
     from cardiax_gb300.stimulus import Protocol, Stimulus
     from cardiax_gb300.tissue import Tissue
@@ -35,7 +37,9 @@ def _mixed_tissues(rng, track=False):
             r, c = rng.integers(0, max(1, H - 10)), rng.integers(0, max(1, W - 10))
             f[r:r + 10, c:c + 10] = 20.0
         proto = Protocol(int(rng.integers(0, 20)), 2, int(rng.integers(150, 400)))
-        t = Tissue((H, W), sets[k % 4], D, [Stimulus(proto, f)], dt=0.01, dx=0.01)
+        # per-tissue time and space steps (the batch holds each tissue's own dt and 1/dx)
+        dt, dx = (0.01, 0.005, 0.02)[k % 3], (0.01, 0.0125)[k % 2]
+        t = Tissue((H, W), sets[k % 4], D, [Stimulus(proto, f)], dt=dt, dx=dx)
         if track:
             t.track_activation(0.5)
         out.append(t)
