@@ -381,3 +381,30 @@ def test_forward_dimensional_vs_oracle():
             e = float(np.abs(_np(getattr(s, var)) - getattr(r, var)).max())
             assert e <= TOL_U_1000, (var, e)
     assert float(states[-1].u.max()) > 0.8
+
+
+def test_stimulus_schedule_on_the_device():
+    """The kernels' protocol test step by step against the reference's schedules (its own
+    stimulate_test.py cases and the floor-mod quirks, tests/golden/stimulus_schedule.json) and
+    negative or fractional periods: the derivative of a resting cell under a one-cell stimulus
+    of 5 is 5 exactly when the protocol is on."""
+    _gpu()
+    import json
+    import os
+    from conftest import GOLDEN
+    from cardiax_gb300 import solve
+    from cardiax_gb300.stimulus import Protocol, Stimulus
+    shp = (8, 8)
+    D = np.full(shp, 1e-3, np.float32)
+    f = np.zeros(shp, np.float32)
+    f[4, 4] = 5.0
+    sched = json.load(open(os.path.join(GOLDEN, "stimulus_schedule.json")))
+    protos = [tuple(rec["protocol"]) for rec in sched.values()]
+    protos += [(10, 3, -20), (7, 4, -13), (5, 2, 12.5), (0, 1.5, 7)]
+    s0 = solve.init(shp)
+    for proto in protos:
+        stims = [Stimulus(Protocol(*proto), f)]
+        got = [t for t in range(300)
+               if abs(float(solve.step(s0, t, P3, D, stims, 0.01).u[4, 4]) - 5.0) < 1e-6]
+        want = [t for t in range(300) if O.stimulus_active(t, *proto)]
+        assert got == want, proto
