@@ -168,7 +168,8 @@ def run_batched(steps: int, reps: int, dev):
             "interleave": tune["interleave"], "packed": tune["packed"],
             "graph_steps": tune["graph_steps"],
             "autotune_ms_per_step": {
-                f"d{k[0]}_rows{k[1]}_{'rr' if k[2][0] else 'runs'}_{'pk' if k[2][1] else 'sc'}"
+                f"d{k[0]}_rows{k[1]}_{('rr' + ('' if k[2][0] == 1 else f'x{k[2][0]}')) if k[2][0] else 'runs'}"
+                f"_{'pk' if k[2][1] else 'sc'}"
                 f"_g{k[3]}": v for k, v in tune["ms_per_step"].items()},
             "workload": "256 tissues, sizes {64^2,128^2,256^2,512^2,256x1024}, sets "
                         "{1A,3,4A,5}, scar D (factor U[0,0.1], floor 1e-4, blur 2), plane or "

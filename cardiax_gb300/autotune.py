@@ -35,8 +35,9 @@ TISSUE_CANDIDATES = (("step", 1, 0), ("step", 1, 1), ("step", 2, 0), ("step", 4,
 
 GRAPH_CANDIDATES = (0, 64)
 TILE_ROW_CANDIDATES = (32, 16)
-# (interleave, packed) of the batched kernel
-OPTION_CANDIDATES = ((True, False), (False, False), (True, True), (False, True))
+# (work order, packed) of the batched kernel: round-robin single items (1) or chunks of 2 or 4
+# neighbouring items, or contiguous runs (0); scalar or packed arithmetic
+OPTION_CANDIDATES = ((1, False), (2, False), (4, False), (0, False), (1, True), (0, True))
 
 
 def _signature(batch: TissueBatch):
@@ -76,7 +77,7 @@ def tune_batch(batch: TissueBatch, trial_steps: int = 256, candidates=GRAPH_CAND
     timings = {}
     configs = [(1, rows, tuple(opt), g) for rows in tile_rows for opt in options
                for g in candidates]
-    configs += [(d, 32, (True, False), g) for d in depths if d != 1 for g in candidates]
+    configs += [(d, 32, (1, False), g) for d in depths if d != 1 for g in candidates]
     for cfg in configs:
         depth, rows, opt, g = cfg
         _set_batch(batch, cfg)

@@ -49,7 +49,7 @@ class TissueBatch:
                ctypes.byref(plan))
         self._plan = plan
         self.tile_rows = 32
-        self.interleave, self.packed = True, False
+        self.interleave, self.packed = 1, False
         self.depth = 1
         if ctas is not None:
             self.set_ctas(ctas)
@@ -60,11 +60,14 @@ class TissueBatch:
         N.call("fk_batch_set_grid", self._plan, int(ctas))
         return self
 
-    def set_options(self, interleave: bool = True, packed: bool = False) -> "TissueBatch":
-        """Work order (CTAs take every G-th item, or contiguous runs of the work list) and
-        arithmetic (packed two-cell or scalar FP32) of the batched kernel; same results."""
-        N.call("fk_batch_set_options", self._plan, int(bool(interleave)), int(bool(packed)))
-        self.interleave, self.packed = bool(interleave), bool(packed)
+    def set_options(self, interleave=True, packed: bool = False) -> "TissueBatch":
+        """Work order and arithmetic of the batched kernel; same results.  ``interleave``:
+        True or 1 -- CTAs take every G-th item of the work list; 2 or 4 -- every G-th chunk of
+        that many neighbouring items; False or 0 -- contiguous runs of the list.  ``packed``:
+        packed two-cell or scalar FP32 arithmetic."""
+        il = int(interleave) if not isinstance(interleave, bool) else int(interleave)
+        N.call("fk_batch_set_options", self._plan, il, int(bool(packed)))
+        self.interleave, self.packed = il, bool(packed)
         return self
 
     def set_depth(self, depth: int) -> "TissueBatch":

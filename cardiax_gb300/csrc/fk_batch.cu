@@ -43,7 +43,9 @@ const TileShape kShape[kShapes] = {{32, 64, 2, fk_batch_launch_rows32},
 struct fk_batch {
     int n = 0, grid = 0, device = -1;
     int shape = 0;  // index into kShape of the tile geometry in use
-    int interleave = 1, packed = 0;  // work order and arithmetic of the batched kernel
+    // work order (0: contiguous runs; k = 1, 2, 4: round-robin in chunks of k items) and
+    // arithmetic of the batched kernel
+    int interleave = 1, packed = 0;
     int depth = 1;                   // Euler steps per launch: 1, or 2 (blocked kernel)
     bool tb_ok = false;              // every tissue can be blocked (and no activation tracking)
     BatchTbMaps *d_tbmaps = nullptr;
@@ -144,6 +146,25 @@ bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) ==
 // Contiguous runs: tissue by tissue (larger first), each tissue's tiles column by column, so
 // that a CTA's run changes tissue rarely and its next item is usually the tile below the
 // current one, whose top halo rows it has just loaded (they are still in L2).
+// Round-robin in chunks of c: the kernel's CTA g of G takes items g, g + G, g + 2G, ...; the
+// list is permuted so that those are c consecutive items of the natural order in turn
+// (natural item x of chunk p = x / c goes to position (p / G) c G + (x % c) G + p % G), so a
+// CTA steps through c neighbouring tiles, mostly of one tissue, before the next chunk.  A last
+// partial block of chunks keeps the natural order.
+void chunk_items(fk_batch::PerShape &P, int c, int G) {
+    const int64_t n = (int64_t)P.h_items.size();
+    if (c <= 1 || G < 1 || n == 0) return;
+    const int64_t full = n / ((int64_t)c * G) * c * G;  // items in whole blocks
+    std::vector<BatchItem> it(P.h_items);
+    std::vector<uint8_t> ed(P.h_edge);
+    for (int64_t x = 0; x < full; ++x) {
+        const int64_t p = x / c, blk = p / G;
+        const int64_t to = blk * c * G + (x % c) * G + p % G;
+        P.h_items[to] = it[x];
+        P.h_edge[to] = ed[x];
+    }
+}
+
 void build_items(fk_batch *b, int q) {
     fk_batch::PerShape &P = b->sp[q];
     const TileShape &ts = kShape[q];
@@ -165,6 +186,7 @@ void build_items(fk_batch *b, int q) {
     if (b->interleave) {
         for (int k : b->order) add(k, 1, false);
         for (int k : b->order) add(k, 0, false);
+        chunk_items(P, b->interleave, b->grid);
     } else {
         for (int k : b->order) add(k, -1, true);
     }
@@ -366,8 +388,15 @@ int fk_batch_set_grid(fk_batch *b, int ctas) {
     if (cudaGetDevice(&dev) != cudaSuccess || dev != b->device) return FK_ERR_CUDA;
     // ordered after the plan's earlier work; the host copies stay alive in the plan
     if (cudaDeviceSynchronize() != cudaSuccess) return FK_ERR_CUDA;
+    b->grid = ctas;
     for (int q = 0; q < kShapes; ++q) {
         fk_batch::PerShape &P = b->sp[q];
+        if (b->interleave > 1) {  // the chunk permutation depends on the CTA count
+            build_items(b, q);
+            if (cudaMemcpy(P.d_items, P.h_items.data(), sizeof(BatchItem) * P.n_items,
+                           cudaMemcpyHostToDevice) != cudaSuccess)
+                return FK_ERR_CUDA;
+        }
         std::vector<int> r;
         make_ranges(P.h_items, P.h_edge, ctas, r);
         if (cudaMemcpy(P.d_ranges, r.data(), sizeof(int) * r.size(), cudaMemcpyHostToDevice) !=
@@ -375,14 +404,15 @@ int fk_batch_set_grid(fk_batch *b, int ctas) {
             return FK_ERR_CUDA;
         P.h_ranges.swap(r);
     }
-    b->grid = ctas;
     release_graph(b);
     return FK_OK;
 }
 
 int fk_batch_set_options(fk_batch *b, int interleave, int packed) {
     if (!b) return FK_ERR_NULL;
-    const int il = interleave ? 1 : 0, pk = packed ? 1 : 0;
+    if (interleave != 0 && interleave != 1 && interleave != 2 && interleave != 4)
+        return FK_ERR_ARGUMENT;
+    const int il = interleave, pk = packed ? 1 : 0;
     if (il != b->interleave || pk != b->packed) release_graph(b);
     b->packed = pk;
     if (il == b->interleave) return FK_OK;

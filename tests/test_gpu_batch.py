@@ -49,7 +49,8 @@ def _mixed_tissues(rng, track=False):
 @pytest.mark.parametrize("graph_steps,n_steps,rows,interleave,packed", [
     (0, 37, 32, True, False), (16, 101, 32, True, False), (64, 64, 32, True, False),
     (0, 37, 16, True, False), (16, 101, 16, True, False), (0, 37, 32, False, False),
-    (16, 101, 32, False, True), (0, 37, 16, False, True), (16, 64, 16, True, True)])
+    (16, 101, 32, False, True), (0, 37, 16, False, True), (16, 64, 16, True, True),
+    (0, 37, 32, 2, False), (16, 101, 16, 4, False), (0, 37, 32, 4, True)])
 def test_batch_matches_single_tissue_bitwise(graph_steps, n_steps, rows, interleave, packed):
     """Every tile geometry (32 x 64, 16 x 64 work items), work order and arithmetic of the
     batched kernel."""
@@ -98,7 +99,7 @@ def test_autotuner_restores_state_and_picks_a_candidate():
     assert res["graph_steps"] in (0, 16) and res["tile_rows"] in (32, 16)
     # one tissue (96 x 257) cannot be blocked: depth 1 only
     assert not batch.can_block() and res["depth"] == 1
-    assert len(res["ms_per_step"]) == 16 and batch.tile_rows == res["tile_rows"]
+    assert len(res["ms_per_step"]) == 24 and batch.tile_rows == res["tile_rows"]
     assert (batch.interleave, batch.packed) == (res["interleave"], res["packed"])
     for t, s in zip(b, before):
         assert torch.equal(t.state, s)
@@ -114,7 +115,9 @@ def test_tile_geometry_switches_mid_run_and_ctas_change():
         t.advance(0, 90)
     batch = TissueBatch(b, graph_steps=16)
     batch.advance(0, 33)
-    batch.set_tile_rows(16).set_options(False, True).advance(33, 61)
+    batch.set_tile_rows(16).set_options(2, False).advance(33, 45)
+    batch.set_ctas(151).advance(45, 50)  # a chunked order is rebuilt for the new CTA count
+    batch.set_options(False, True).advance(50, 61)
     batch.set_ctas(97).set_tile_rows(32).set_options(True, True).advance(61, 90)
     torch.cuda.synchronize()
     for x, y in zip(a, b):
