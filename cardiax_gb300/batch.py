@@ -62,8 +62,8 @@ class TissueBatch:
 
     def set_options(self, interleave=True, packed: bool = False) -> "TissueBatch":
         """Work order and arithmetic of the batched kernel; same results.  ``interleave``:
-        True or 1 -- CTAs take every G-th item of the work list; 2 or 4 -- every G-th chunk of
-        that many neighbouring items; False or 0 -- contiguous runs of the list.  ``packed``:
+        True or 1 -- CTAs take every G-th item of the work list; 2, 4 or 8 -- every G-th chunk
+        of that many neighbouring items; False or 0 -- contiguous runs of the list.  ``packed``:
         packed two-cell or scalar FP32 arithmetic."""
         il = int(interleave) if not isinstance(interleave, bool) else int(interleave)
         N.call("fk_batch_set_options", self._plan, il, int(bool(packed)))

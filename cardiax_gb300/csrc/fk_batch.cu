@@ -43,7 +43,7 @@ const TileShape kShape[kShapes] = {{32, 64, 2, fk_batch_launch_rows32},
 struct fk_batch {
     int n = 0, grid = 0, device = -1;
     int shape = 0;  // index into kShape of the tile geometry in use
-    // work order (0: contiguous runs; k = 1, 2, 4: round-robin in chunks of k items) and
+    // work order (0: contiguous runs; k = 1, 2, 4, 8: round-robin in chunks of k items) and
     // arithmetic of the batched kernel
     int interleave = 1, packed = 0;
     int depth = 1;                   // Euler steps per launch: 1, or 2 (blocked kernel)
@@ -410,7 +410,8 @@ int fk_batch_set_grid(fk_batch *b, int ctas) {
 
 int fk_batch_set_options(fk_batch *b, int interleave, int packed) {
     if (!b) return FK_ERR_NULL;
-    if (interleave != 0 && interleave != 1 && interleave != 2 && interleave != 4)
+    if (interleave != 0 && interleave != 1 && interleave != 2 && interleave != 4 &&
+        interleave != 8)
         return FK_ERR_ARGUMENT;
     const int il = interleave, pk = packed ? 1 : 0;
     if (il != b->interleave || pk != b->packed) release_graph(b);

@@ -280,8 +280,8 @@ int fk_batch_set_grid(fk_batch *plan, int ctas);
 int fk_batch_set_tile_rows(fk_batch *plan, int rows);
 
 /* Work order and arithmetic of the batched kernel: interleave = 1 (the default) deals the
- * work list round-robin to the CTAs (edge tiles first), 2 or 4 deals it round-robin in chunks of
- * that many neighbouring items (a CTA's consecutive items then mostly share a tissue), 0 gives
+ * work list round-robin to the CTAs (edge tiles first), 2, 4 or 8 deals it round-robin in chunks
+ * of that many neighbouring items (a CTA's consecutive items then mostly share a tissue), 0 gives
  * each CTA a contiguous run of it (tissue by tissue, balanced by cost); other values:
  * FK_ERR_ARGUMENT.  packed != 0 uses packed two-cell FP32 instructions (default 0: scalar).
  * Same bits either way; tuning knobs.  No counterpart in the reference. */
